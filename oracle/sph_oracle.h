@@ -1,0 +1,73 @@
+/* CPU restatement ("port") of the reference SPH step, in plain C with OpenMP.
+ *
+ * TEST INFRASTRUCTURE ONLY: this is the oracle.  Only tests/, __graft_entry__.smoke() and
+ * bench.py's CPU-baseline / reference arm may load it, and only as the checker or the
+ * timed CPU baseline -- never as part of the product path.
+ *
+ * Parameter blocks are 16 floats in SPHParameters field order (src/sph_engine.h:14-34):
+ *   rest_density, gas_constant, viscosity, smoothing_length, particle_mass, timestep,
+ *   gravity, damping, CFL_factor, xmin, xmax, ymin, ymax, zmin, zmax,
+ *   neighbor_search_radius
+ * Vectors are flat float arrays, 3 floats per particle, in insertion order.
+ */
+#ifndef SPH_ORACLE_H
+#define SPH_ORACLE_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Neighbour lists exactly as SpatialHash::query_squared produces them
+ * (src/spatial_hash.cpp:31-57): order, self included.  counts[n]; idx (optional) gets the
+ * concatenated lists.  Returns the total number of entries. */
+int64_t orc_query(size_t n, const float* pos, float cell_size, float radius, int64_t* counts,
+                  int64_t* idx);
+
+/* One evaluation of density, pressure and acceleration on a given state, in FP32 with the
+ * reference's operation order (src/sph_engine.cpp:203-244, 370-443). */
+void orc_fields(size_t n, const float* pos, const float* vel, const float* mass,
+                const float* params16, float* rho, float* P, float* acc);
+
+/* The same evaluation in FP64 over the same (FP32-defined) neighbour sets: the
+ * high-precision reference for error figures.  Optionally (sum_abs != NULL) also returns,
+ * per particle and component, the sum of |term| of the acceleration's pair terms divided
+ * by m_i: the conditioning scale against which FP32 force errors are judged. */
+void orc_fields_f64(size_t n, const float* pos, const float* vel, const float* mass,
+                    const float* params16, double* rho, double* P, double* acc,
+                    double* sum_abs);
+
+/* ---- engine: restatement of SPHEngine state and step (src/sph_engine.cpp:13-353) ---- */
+typedef struct orc_engine orc_engine;
+orc_engine* orc_engine_new(size_t capacity);
+void orc_engine_free(orc_engine* e);
+void orc_engine_initialize(orc_engine* e, const float* params16);
+/* Appends particles; beyond capacity they are dropped (src/particle.cpp:26-33).
+ * vel may be NULL (zero velocity). */
+void orc_engine_add(orc_engine* e, size_t n, const float* pos, const float* vel,
+                    const float* mass);
+void orc_engine_clear(orc_engine* e);
+void orc_engine_step(orc_engine* e, float dt);
+size_t orc_engine_size(const orc_engine* e);
+float orc_engine_time(const orc_engine* e);
+uint64_t orc_engine_step_count(const orc_engine* e);
+/* pos/vel/acc: 3*size floats (acc = the engine's accelerations_ buffer);
+ * rho/P: capacity floats (get_densities()/get_pressures()). Any pointer may be NULL. */
+void orc_engine_get(const orc_engine* e, float* pos, float* vel, float* acc, float* rho,
+                    float* P);
+/* Overwrites the state of the first size() particles (pos/vel may be NULL). */
+void orc_engine_set_state(orc_engine* e, const float* pos, const float* vel);
+/* total_mass, total_energy, mass_error, energy_error, max_neighbors,
+ * total_neighbor_queries (src/sph_engine.cpp:178-200). */
+void orc_engine_diag(const orc_engine* e, double* out6);
+/* Last CFL timestep the engine computed (0 if none). */
+float orc_engine_last_dt(const orc_engine* e);
+
+int orc_max_threads(void);
+void orc_set_threads(int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
