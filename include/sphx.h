@@ -1,0 +1,175 @@
+/* sphx -- C ABI of the GB300 (sm_103a) SPH step.
+ *
+ * This is the boundary behind which the reference's SPHEngine::step runs on the GPU.
+ * The reference has no FFI of its own for this path: its C++ SPHEngine calls the phases
+ * directly (src/sph_engine.cpp:93-144) and its pybind11 module binds SPHEngine methods
+ * (python/bindings.cpp:83-139).  Each entry point below names the reference interface it
+ * stands in for.  Plain pointers and sizes only; no C++ or framework types cross it.
+ *
+ * Conventions
+ *  - Every function returns SPHX_OK (0) or a negative SPHX_ERR_* code; no exception ever
+ *    crosses the ABI.  sphx_strerror() turns a code into text.
+ *  - One context per host thread.  A context owns all of its device memory and one CUDA
+ *    stream (or uses the caller's, see sphx_set_stream).  Calls are stream-ordered:
+ *    sphx_step() only enqueues work; the download/stats/time calls synchronise.
+ *    Errors detected on the device are reported by the next synchronising call.
+ *  - Vectors are 3 floats per particle; all host-side arrays are in insertion order
+ *    (particle i is the i-th particle uploaded), like the reference's ParticleSystem.
+ *  - Arithmetic is IEEE FP32 with the reference's own operation order.  In
+ *    SPHX_MODE_EXACT every field of a step (neighbour lists and their order, density,
+ *    pressure, acceleration, position, velocity, time) is bit-identical to the reference
+ *    core built with IEEE float semantics (no FMA contraction, no fast-math).
+ */
+#ifndef SPHX_H
+#define SPHX_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPHX_ABI_VERSION 1
+
+/* status codes */
+#define SPHX_OK 0
+#define SPHX_ERR_INVALID_ARG (-1)  /* null pointer, bad size, bad parameter */
+#define SPHX_ERR_OOM (-2)          /* device or pinned-host allocation failed */
+#define SPHX_ERR_CUDA (-3)         /* a CUDA runtime call failed (no device, launch error) */
+#define SPHX_ERR_TIMEOUT (-4)      /* a bounded device-side wait gave up */
+#define SPHX_ERR_CAPACITY (-5)     /* more particles than the context's capacity */
+#define SPHX_ERR_NOT_READY (-6)    /* no parameters or no particles yet */
+#define SPHX_ERR_DOMAIN (-7)       /* occupied cell box too large for the cell grid */
+#define SPHX_ERR_OVERFLOW (-8)     /* caller's output buffer too small */
+
+/* SPHParameters (src/sph_engine.h:14-34), same fields, same order, same meaning. */
+typedef struct sphx_params {
+    float rest_density;
+    float gas_constant;
+    float viscosity;
+    float smoothing_length;
+    float particle_mass;
+    float timestep;
+    float gravity;
+    float damping;
+    float cfl_factor;
+    float xmin, xmax, ymin, ymax, zmin, zmax;
+    float neighbor_search_radius;
+} sphx_params;
+
+/* mode */
+#define SPHX_MODE_EXACT 0 /* reference operation order and IEEE ops: bit-identical step */
+
+typedef struct sphx_tuning {
+    int mode;              /* SPHX_MODE_* (default EXACT) */
+    int warps_per_block;   /* neighbour-pass CTA size in warps; 0 = default (4) */
+    int blocks_per_sm;     /* persistent CTAs per SM for the neighbour passes; 0 = auto */
+    int64_t max_grid_cells;/* cap on the dense cell grid (cells); 0 = default */
+    int profile;           /* 1 = time each phase with CUDA events (read back lazily) */
+} sphx_tuning;
+
+/* PerformanceStats (src/sph_engine.h:51-59) plus GPU-side diagnostics. */
+typedef struct sphx_stats {
+    double total_time;               /* seconds, accumulated like the reference (the
+                                        time fields are filled when tuning.profile = 1) */
+    double neighbor_search_time;     /* grid build: bbox, keys, sort, reorder, cells */
+    double density_computation_time; /* density + pressure pass */
+    double force_computation_time;   /* force pass (integration is fused into it) */
+    double integration_time;         /* 0: fused into the force pass */
+    uint64_t max_neighbors;          /* max |N(i)| including self, since last reset */
+    uint64_t total_neighbor_queries; /* particles queried, since last reset */
+    uint64_t steps;                  /* steps taken by this context */
+    float current_time;              /* sum of dt (float, like SPHEngine::current_time_) */
+    float last_dt;                   /* dt used by the last step */
+    uint32_t occupied_cells;         /* last step: occupied search cells */
+    uint32_t max_cell_occupancy;     /* last step: particles in the fullest cell */
+    uint32_t nonfinite_particles;    /* last step: particles with a NaN/inf coordinate */
+    uint32_t grid_cells;             /* last step: cells in the dense grid */
+    /* FP64 reductions over the state after the last step */
+    double sum_mass;
+    double momentum[3];
+    double kinetic_energy;           /* sum 0.5 m |v|^2 */
+    double potential_energy;         /* sum -m g y (gravity acts along y) */
+    double sum_density;              /* sum rho_i, FP64 (get_total_mass = sum * h^3) */
+    uint64_t kernel_launches;        /* GPU kernels launched by steps/evals of this context */
+} sphx_stats;
+
+typedef struct sphx_ctx sphx_ctx;
+
+/* Library ABI version (SPHX_ABI_VERSION). */
+int sphx_version(void);
+const char* sphx_strerror(int code);
+
+/* Creates a context able to hold `capacity` particles on the current CUDA device.
+ * Stands in for SPHEngine(size_t max_particles) (src/sph_engine.h:91, cpp:13-18).
+ * tuning may be NULL (defaults). */
+int sphx_create(sphx_ctx** out, size_t capacity, const sphx_tuning* tuning);
+void sphx_destroy(sphx_ctx* ctx);
+
+/* Launch on the caller's CUDA stream (a cudaStream_t passed as void*); NULL restores the
+ * context's own stream. */
+int sphx_set_stream(sphx_ctx* ctx, void* cuda_stream);
+
+/* SPHEngine::initialize / set_parameters (src/sph_engine.cpp:20-33, 152-156): the step
+ * uses params exactly as given (search radius = neighbor_search_radius; the 2h rule of
+ * set_smoothing_length is the host engine's business). */
+int sphx_set_params(sphx_ctx* ctx, const sphx_params* params);
+
+/* Replaces the particle set with n particles from host memory (the device side of
+ * SPHEngine::add_particles / clear_particles, src/sph_engine.cpp:83-91).  vel may be NULL
+ * (zero).  n > capacity -> SPHX_ERR_CAPACITY (the host engine applies the reference's
+ * drop-with-warning rule before calling).  The acceleration used by the CFL rule for
+ * particle 0 persists across uploads, as the reference's accelerations_ buffer does. */
+int sphx_upload(sphx_ctx* ctx, size_t n, const float* pos_xyz, const float* vel_xyz,
+                const float* mass);
+
+/* SPHEngine::step(float dt) (src/sph_engine.cpp:93-144): dt <= 0 selects the CFL
+ * timestep (compute_cfl_timestep, cpp:312-333), computed on the device.  A no-op when no
+ * particles are loaded (cpp:94).  Asynchronous. */
+int sphx_step(sphx_ctx* ctx, float dt);
+
+/* Runs the neighbour search, density, pressure and force phases of a step on the current
+ * state without integrating (positions and velocities unchanged): the state the
+ * reference's compute_densities / compute_pressures / compute_forces produce
+ * (src/sph_engine.cpp:203-244).  Read the result with sphx_download. */
+int sphx_eval(sphx_ctx* ctx);
+
+/* Copies fields of the current state to host memory in insertion order; synchronises.
+ * SPHEngine::get_positions / get_velocities / get_densities / get_pressures
+ * (src/sph_engine.h:133-136).  Any pointer may be NULL.  rho/p/acc are those of the last
+ * step or eval (acc is the reference's accelerations_ buffer). */
+int sphx_download(sphx_ctx* ctx, float* pos_xyz, float* vel_xyz, float* rho, float* pressure,
+                  float* acc_xyz);
+
+/* Number of particles currently loaded. */
+int sphx_size(sphx_ctx* ctx, size_t* n);
+
+/* current_time_ and the last dt (synchronises). */
+int sphx_get_time(sphx_ctx* ctx, float* current_time, float* last_dt);
+/* Sets current_time_ (SPHEngine::clear_particles resets it to 0, cpp:87-91). */
+int sphx_set_time(sphx_ctx* ctx, float current_time);
+
+/* get_performance_stats / reset_performance_stats (src/sph_engine.h:124-125), plus the
+ * FP64 conservation sums (synchronises). */
+int sphx_get_stats(sphx_ctx* ctx, sphx_stats* out);
+int sphx_reset_stats(sphx_ctx* ctx);
+
+/* Device-side copy of the current positions/velocities, and its restore: lets a caller
+ * re-run steps from one state without host traffic (fresh-state benchmarking). */
+int sphx_snapshot(sphx_ctx* ctx);
+int sphx_restore(sphx_ctx* ctx);
+
+/* Neighbour lists of the current state, as SpatialHash::query_squared returns them for
+ * SPHEngine::update_neighbor_lists (src/spatial_hash.cpp:31-57, src/sph_engine.cpp:335-353):
+ * counts[i] = |N(i)| (self included); when idx != NULL and *total_inout >= the number of
+ * pairs, idx receives the concatenated lists (insertion indices) in the reference's
+ * order.  On return *total_inout holds the number of pairs (SPHX_ERR_OVERFLOW when idx
+ * was too small).  Test hook; synchronises.  It rebuilds the cell grid, so the
+ * rho/pressure/acc fields of the previous step are no longer downloadable afterwards
+ * (sphx_download returns zeros for them until the next step or eval). */
+int sphx_debug_pairs(sphx_ctx* ctx, int64_t* counts, int64_t* idx, size_t* total_inout);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPHX_H */

@@ -1,0 +1,541 @@
+// C ABI of the sm_103a SPH step (include/sphx.h): context lifetime, device memory,
+// host<->device transfers and the step's launch sequence.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "sphx_internal.cuh"
+
+using namespace sphx;
+
+struct sphx_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    size_t capacity = 0;
+    size_t n = 0;
+    sphx_tuning tuning{};
+    sphx_params params{};
+    bool have_params = false;
+    bool have_fields = false;  // rho/P/acc of the current particle set exist
+    StepConst sc{};
+    Buffers b{};
+    DevState* ds = nullptr;
+    float* stage = nullptr;    // 7 * capacity floats
+    float4* snap_pos = nullptr;
+    float4* snap_vel = nullptr;
+    LaunchCtx L{};
+    uint64_t steps = 0;
+    uint64_t queries = 0;
+    uint64_t launches = 0;  // kernels this context has launched for steps/evals
+    double t_total = 0, t_nb = 0, t_den = 0, t_force = 0;
+    // per-phase timing: events recorded into a ring, read back only when a slot is reused
+    // or the stats are requested, so profiling adds no per-step host sync
+    static constexpr int kProfRing = 64;
+    struct ProfSlot {
+        cudaEvent_t ev[5];
+        bool pending;
+    } prof[kProfRing] = {};
+    int prof_head = 0;
+};
+
+namespace {
+
+constexpr int kDefaultWarpsPerBlock = 4;
+
+int cuda_fail(cudaError_t e) {
+    if (e == cudaErrorMemoryAllocation) return SPHX_ERR_OOM;
+    return SPHX_ERR_CUDA;
+}
+
+#define SPHX_CUDA(call)                            \
+    do {                                           \
+        cudaError_t e_ = (call);                   \
+        if (e_ != cudaSuccess) return cuda_fail(e_); \
+    } while (0)
+
+template <class T>
+int dmalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return cuda_fail(e);
+    }
+    return SPHX_OK;
+}
+
+// Host copy of CubicSplineKernel::W_3d (kernels.cpp:58-66) for the self term W(0); this
+// file is compiled with -ffp-contract=off so float expressions round like the reference.
+float host_cubic_w(float sigma, float q) {
+    if (q >= 0.0f && q <= 1.0f) {
+        return sigma * (2.0f / 3.0f - q * q + 0.5f * q * q * q);
+    } else if (q > 1.0f && q <= 2.0f) {
+        const float tmp = 2.0f - q;
+        return sigma * (1.0f / 6.0f * tmp * tmp * tmp);
+    }
+    return 0.0f;
+}
+
+void fill_step_const(sphx_ctx* c) {
+    const sphx_params& p = c->params;
+    StepConst& s = c->sc;
+    s.n = (int)c->n;
+    // SpatialHash::set_cell_size(neighbor_search_radius): inv = 1.0f / cell
+    s.inv_cell = 1.0f / p.neighbor_search_radius;
+    s.r2 = p.neighbor_search_radius * p.neighbor_search_radius;
+    // CubicSplineKernel(h): h_sq = h*h, sigma_3d = 1 / (float(pi) * h * h * h)
+    const float h = p.smoothing_length;
+    s.h = h;
+    s.h_sq = h * h;
+    s.sigma = 1.0f / (static_cast<float>(M_PI) * h * h * h);
+    // W(vec3(0)): q = length(0) / h
+    const float q0 = std::sqrt(0.0f) / h;
+    s.w0 = host_cubic_w(s.sigma, q0);
+    s.rest = p.rest_density;
+    s.gas = p.gas_constant;
+    s.visc = p.viscosity;
+    s.grav = p.gravity;
+    s.damping = p.damping;
+    s.cfl = p.cfl_factor;
+    s.timestep = p.timestep;
+    s.lo[0] = p.xmin;
+    s.hi[0] = p.xmax;
+    s.lo[1] = p.ymin;
+    s.hi[1] = p.ymax;
+    s.lo[2] = p.zmin;
+    s.hi[2] = p.zmax;
+}
+
+void free_all(sphx_ctx* c) {
+    Buffers& b = c->b;
+    void* ptrs[] = {b.pos4, b.vel4,   b.pos4_s, b.vel4_s,     b.aux4_s,    b.acc4_s,
+                    b.key[0], b.key[1], b.val[0], b.val[1],   b.key_s,     b.id_s,
+                    b.off,  b.tile_start, b.hist, b.scan_part, b.diag_part, c->ds,
+                    c->stage, c->snap_pos, c->snap_vel};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    for (auto& slot : c->prof)
+        for (auto& e : slot.ev)
+            if (e) cudaEventDestroy(e);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+}
+
+// Adds one recorded step's phase times to the accumulators (waits for it if needed).
+int drain_slot(sphx_ctx* c, sphx_ctx::ProfSlot& slot) {
+    if (!slot.pending) return SPHX_OK;
+    slot.pending = false;
+    SPHX_CUDA(cudaEventSynchronize(slot.ev[4]));
+    float ms[4];
+    for (int k = 0; k < 4; ++k) SPHX_CUDA(cudaEventElapsedTime(&ms[k], slot.ev[k], slot.ev[k + 1]));
+    c->t_nb += ms[0] * 1e-3;
+    c->t_den += ms[1] * 1e-3;
+    c->t_force += ms[2] * 1e-3;
+    c->t_total += (ms[0] + ms[1] + ms[2] + ms[3]) * 1e-3;
+    return SPHX_OK;
+}
+
+int drain_all(sphx_ctx* c) {
+    for (auto& slot : c->prof) {
+        const int rc = drain_slot(c, slot);
+        if (rc) return rc;
+    }
+    return SPHX_OK;
+}
+
+int sync_status(sphx_ctx* c) {
+    SPHX_CUDA(cudaStreamSynchronize(c->stream));
+    SPHX_CUDA(cudaGetLastError());
+    int st[2] = {0, 0};
+    SPHX_CUDA(cudaMemcpy(st, c->ds, sizeof(int), cudaMemcpyDeviceToHost));
+    return st[0];
+}
+
+int enter(sphx_ctx* c) {
+    if (!c) return SPHX_ERR_INVALID_ARG;
+    SPHX_CUDA(cudaSetDevice(c->device));
+    return SPHX_OK;
+}
+
+int run_phases(sphx_ctx* c, float dt, bool integrate) {
+    fill_step_const(c);
+    sphx_ctx::ProfSlot* slot = nullptr;
+    if (c->tuning.profile) {
+        slot = &c->prof[c->prof_head];
+        c->prof_head = (c->prof_head + 1) % sphx_ctx::kProfRing;
+        const int rc = drain_slot(c, *slot);
+        if (rc) return rc;
+        SPHX_CUDA(cudaEventRecord(slot->ev[0], c->stream));
+    }
+    int k = launch_begin_step(c->L, c->ds, 1);
+    if (integrate) k += launch_cfl(c->L, c->sc, c->b, c->ds, dt);
+    k += launch_build_grid(c->L, c->sc, c->b, c->ds);
+    if (slot) SPHX_CUDA(cudaEventRecord(slot->ev[1], c->stream));
+    k += launch_density(c->L, c->sc, c->b, c->ds);
+    if (slot) SPHX_CUDA(cudaEventRecord(slot->ev[2], c->stream));
+    k += launch_force(c->L, c->sc, c->b, c->ds, integrate ? 1 : 0);
+    if (slot) SPHX_CUDA(cudaEventRecord(slot->ev[3], c->stream));
+    if (integrate) k += launch_diag(c->L, c->sc, c->b, c->ds);
+    if (slot) {
+        SPHX_CUDA(cudaEventRecord(slot->ev[4], c->stream));
+        slot->pending = true;
+    }
+    SPHX_CUDA(cudaGetLastError());
+    c->launches += (uint64_t)k;
+    c->have_fields = true;
+    return SPHX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sphx_version(void) { return SPHX_ABI_VERSION; }
+
+const char* sphx_strerror(int code) {
+    switch (code) {
+        case SPHX_OK: return "ok";
+        case SPHX_ERR_INVALID_ARG: return "invalid argument";
+        case SPHX_ERR_OOM: return "out of memory";
+        case SPHX_ERR_CUDA: return "CUDA runtime error";
+        case SPHX_ERR_TIMEOUT: return "device-side wait timed out";
+        case SPHX_ERR_CAPACITY: return "particle capacity exceeded";
+        case SPHX_ERR_NOT_READY: return "parameters or particles not set";
+        case SPHX_ERR_DOMAIN: return "occupied cell box exceeds the cell grid capacity";
+        case SPHX_ERR_OVERFLOW: return "output buffer too small";
+        default: return "unknown sphx error";
+    }
+}
+
+int sphx_create(sphx_ctx** out, size_t capacity, const sphx_tuning* tuning) {
+    if (!out) return SPHX_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (capacity == 0 || capacity > (size_t)0x7fffffff - 64) return SPHX_ERR_INVALID_ARG;
+    int dev_count = 0;
+    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) return SPHX_ERR_CUDA;
+    sphx_ctx* c = new (std::nothrow) sphx_ctx();
+    if (!c) return SPHX_ERR_OOM;
+    if (tuning) c->tuning = *tuning;
+    if (c->tuning.warps_per_block <= 0 || c->tuning.warps_per_block > 4)
+        c->tuning.warps_per_block = kDefaultWarpsPerBlock;
+    int rc = SPHX_OK;
+    auto fail = [&](int code) {
+        free_all(c);
+        delete c;
+        return code;
+    };
+    if (cudaGetDevice(&c->device) != cudaSuccess) return fail(SPHX_ERR_CUDA);
+    if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(SPHX_ERR_CUDA);
+    c->stream = c->own_stream;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    c->L.num_sms = sms > 0 ? sms : 1;
+    c->L.warps_per_block = c->tuning.warps_per_block;
+    c->L.blocks_per_sm = c->tuning.blocks_per_sm;
+    c->L.stream = c->stream;
+    c->capacity = capacity;
+    int64_t max_cells = c->tuning.max_grid_cells;
+    if (max_cells <= 0) {
+        max_cells = (int64_t)capacity * 4;
+        if (max_cells < (int64_t)1 << 24) max_cells = (int64_t)1 << 24;
+    }
+    if (max_cells > ((int64_t)1 << 31) - 4) max_cells = ((int64_t)1 << 31) - 4;
+    c->sc.max_cells = (uint32_t)max_cells;
+    Buffers& b = c->b;
+    const size_t C = capacity;
+    b.radix_blocks = (int)((C + kRadixTileN - 1) / kRadixTileN);
+    const size_t hist_n = (size_t)b.radix_blocks * kRadixBuckets;
+    const size_t part_a = (hist_n + kScanTileN - 1) / kScanTileN;
+    const size_t part_b = (C + kScanTileN - 1) / kScanTileN;
+    b.scan_part_cap = (int)((part_a > part_b ? part_a : part_b) + 1);
+    b.diag_blocks = c->L.num_sms * 2;
+    if ((rc = dmalloc(&b.pos4, C)) || (rc = dmalloc(&b.vel4, C)) || (rc = dmalloc(&b.pos4_s, C)) ||
+        (rc = dmalloc(&b.vel4_s, C)) || (rc = dmalloc(&b.aux4_s, C)) ||
+        (rc = dmalloc(&b.acc4_s, C)) || (rc = dmalloc(&b.key[0], C)) ||
+        (rc = dmalloc(&b.key[1], C)) || (rc = dmalloc(&b.val[0], C)) ||
+        (rc = dmalloc(&b.val[1], C)) || (rc = dmalloc(&b.key_s, C)) ||
+        (rc = dmalloc(&b.id_s, C)) || (rc = dmalloc(&b.off, (size_t)max_cells + 2)) ||
+        (rc = dmalloc(&b.tile_start, C)) || (rc = dmalloc(&b.hist, hist_n)) ||
+        (rc = dmalloc(&b.scan_part, (size_t)b.scan_part_cap)) ||
+        (rc = dmalloc(&b.diag_part, (size_t)b.diag_blocks * kDiagSums)) ||
+        (rc = dmalloc(&c->ds, 1)) || (rc = dmalloc(&c->stage, 7 * C)))
+        return fail(rc);
+    if (cudaMemset(c->ds, 0, sizeof(DevState)) != cudaSuccess) return fail(SPHX_ERR_CUDA);
+    if (cudaMemset(b.aux4_s, 0, C * sizeof(float4)) != cudaSuccess ||
+        cudaMemset(b.acc4_s, 0, C * sizeof(float4)) != cudaSuccess)
+        return fail(SPHX_ERR_CUDA);
+    if (c->tuning.profile)
+        for (auto& slot : c->prof)
+            for (auto& e : slot.ev)
+                if (cudaEventCreate(&e) != cudaSuccess) return fail(SPHX_ERR_CUDA);
+    *out = c;
+    return SPHX_OK;
+}
+
+void sphx_destroy(sphx_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_all(c);
+    delete c;
+}
+
+int sphx_set_stream(sphx_ctx* c, void* stream) {
+    int rc = enter(c);
+    if (rc) return rc;
+    SPHX_CUDA(cudaStreamSynchronize(c->stream));
+    c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+    c->L.stream = c->stream;
+    return SPHX_OK;
+}
+
+int sphx_set_params(sphx_ctx* c, const sphx_params* p) {
+    int rc = enter(c);
+    if (rc) return rc;
+    if (!p) return SPHX_ERR_INVALID_ARG;
+    const float r = p->neighbor_search_radius;
+    if (!(r > 0.0f) || !std::isfinite(r) || !std::isfinite(1.0f / r)) return SPHX_ERR_INVALID_ARG;
+    c->params = *p;
+    c->have_params = true;
+    return SPHX_OK;
+}
+
+int sphx_upload(sphx_ctx* c, size_t n, const float* pos, const float* vel, const float* mass) {
+    int rc = enter(c);
+    if (rc) return rc;
+    if (n > c->capacity) return SPHX_ERR_CAPACITY;
+    if (n > 0 && (!pos || !mass)) return SPHX_ERR_INVALID_ARG;
+    float* s_pos = c->stage;
+    float* s_vel = c->stage + 3 * c->capacity;
+    float* s_mass = c->stage + 6 * c->capacity;
+    if (n > 0) {
+        SPHX_CUDA(cudaMemcpyAsync(s_pos, pos, 3 * n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+        if (vel)
+            SPHX_CUDA(cudaMemcpyAsync(s_vel, vel, 3 * n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+        SPHX_CUDA(cudaMemcpyAsync(s_mass, mass, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+        launch_pack(c->L, (int)n, s_pos, vel ? s_vel : nullptr, s_mass, c->b.pos4, c->b.vel4);
+        SPHX_CUDA(cudaGetLastError());
+    }
+    c->n = n;
+    c->have_fields = false;
+    return SPHX_OK;
+}
+
+int sphx_size(sphx_ctx* c, size_t* n) {
+    if (!c || !n) return SPHX_ERR_INVALID_ARG;
+    *n = c->n;
+    return SPHX_OK;
+}
+
+int sphx_step(sphx_ctx* c, float dt) {
+    int rc = enter(c);
+    if (rc) return rc;
+    if (c->n == 0) return SPHX_OK;  // SPHEngine::step returns when empty (cpp:94)
+    if (!c->have_params) return SPHX_ERR_NOT_READY;
+    rc = run_phases(c, dt, true);
+    if (rc) return rc;
+    c->steps++;
+    c->queries += c->n;
+    return SPHX_OK;
+}
+
+int sphx_eval(sphx_ctx* c) {
+    int rc = enter(c);
+    if (rc) return rc;
+    if (c->n == 0) return SPHX_OK;
+    if (!c->have_params) return SPHX_ERR_NOT_READY;
+    return run_phases(c, 0.0f, false);
+}
+
+int sphx_download(sphx_ctx* c, float* pos, float* vel, float* rho, float* pressure, float* acc) {
+    int rc = enter(c);
+    if (rc) return rc;
+    rc = sync_status(c);
+    if (rc) return rc;
+    const size_t n = c->n;
+    if (n == 0) return SPHX_OK;
+    float* s0 = c->stage;
+    float* s1 = c->stage + 3 * c->capacity;
+    if (pos || vel) {
+        launch_unpack_state(c->L, (int)n, c->b.pos4, c->b.vel4, pos ? s0 : nullptr, vel ? s1 : nullptr);
+        SPHX_CUDA(cudaGetLastError());
+        if (pos) SPHX_CUDA(cudaMemcpyAsync(pos, s0, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+        if (vel) SPHX_CUDA(cudaMemcpyAsync(vel, s1, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+        SPHX_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    if (rho || pressure || acc) {
+        float* s_rho = c->stage;
+        float* s_p = c->stage + c->capacity;
+        float* s_acc = c->stage + 2 * c->capacity;
+        if (c->have_fields) {
+            launch_unpack_sorted(c->L, (int)n, c->b.id_s, c->b.aux4_s, c->b.acc4_s,
+                                 rho ? s_rho : nullptr, pressure ? s_p : nullptr,
+                                 acc ? s_acc : nullptr);
+            SPHX_CUDA(cudaGetLastError());
+        } else {
+            SPHX_CUDA(cudaMemsetAsync(c->stage, 0, 5 * n * sizeof(float), c->stream));
+        }
+        if (rho) SPHX_CUDA(cudaMemcpyAsync(rho, s_rho, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+        if (pressure) SPHX_CUDA(cudaMemcpyAsync(pressure, s_p, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+        if (acc) SPHX_CUDA(cudaMemcpyAsync(acc, s_acc, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+        SPHX_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    return SPHX_OK;
+}
+
+int sphx_get_time(sphx_ctx* c, float* current_time, float* last_dt) {
+    int rc = enter(c);
+    if (rc) return rc;
+    SPHX_CUDA(cudaStreamSynchronize(c->stream));
+    DevState s;
+    SPHX_CUDA(cudaMemcpy(&s, c->ds, sizeof(DevState), cudaMemcpyDeviceToHost));
+    if (current_time) *current_time = s.time;
+    if (last_dt) *last_dt = s.dt;
+    return SPHX_OK;
+}
+
+int sphx_set_time(sphx_ctx* c, float t) {
+    int rc = enter(c);
+    if (rc) return rc;
+    SPHX_CUDA(cudaStreamSynchronize(c->stream));
+    SPHX_CUDA(cudaMemcpy(reinterpret_cast<char*>(c->ds) + offsetof(DevState, time), &t,
+                         sizeof(float), cudaMemcpyHostToDevice));
+    return SPHX_OK;
+}
+
+int sphx_get_stats(sphx_ctx* c, sphx_stats* out) {
+    int rc = enter(c);
+    if (rc) return rc;
+    if (!out) return SPHX_ERR_INVALID_ARG;
+    SPHX_CUDA(cudaStreamSynchronize(c->stream));
+    rc = drain_all(c);
+    if (rc) return rc;
+    DevState s;
+    SPHX_CUDA(cudaMemcpy(&s, c->ds, sizeof(DevState), cudaMemcpyDeviceToHost));
+    std::memset(out, 0, sizeof(*out));
+    out->total_time = c->t_total;
+    out->neighbor_search_time = c->t_nb;
+    out->density_computation_time = c->t_den;
+    out->force_computation_time = c->t_force;
+    out->integration_time = 0.0;
+    out->max_neighbors = s.max_nn;
+    out->total_neighbor_queries = c->queries;
+    out->steps = c->steps;
+    out->current_time = s.time;
+    out->last_dt = s.dt;
+    out->occupied_cells = s.occupied;
+    out->max_cell_occupancy = s.max_occ;
+    out->nonfinite_particles = s.nonfinite;
+    out->grid_cells = s.ncells;
+    out->sum_mass = s.sums[0];
+    out->momentum[0] = s.sums[1];
+    out->momentum[1] = s.sums[2];
+    out->momentum[2] = s.sums[3];
+    out->kinetic_energy = s.sums[4];
+    out->potential_energy = s.sums[5];
+    out->sum_density = s.sums[6];
+    out->kernel_launches = c->launches;
+    return s.status;
+}
+
+int sphx_reset_stats(sphx_ctx* c) {
+    int rc = enter(c);
+    if (rc) return rc;
+    SPHX_CUDA(cudaStreamSynchronize(c->stream));
+    rc = drain_all(c);
+    if (rc) return rc;
+    c->t_total = c->t_nb = c->t_den = c->t_force = 0.0;
+    c->queries = 0;
+    unsigned long long z = 0;
+    SPHX_CUDA(cudaMemcpy(reinterpret_cast<char*>(c->ds) + offsetof(DevState, max_nn), &z,
+                         sizeof(z), cudaMemcpyHostToDevice));
+    return SPHX_OK;
+}
+
+int sphx_snapshot(sphx_ctx* c) {
+    int rc = enter(c);
+    if (rc) return rc;
+    if (!c->snap_pos) {
+        if ((rc = dmalloc(&c->snap_pos, c->capacity)) || (rc = dmalloc(&c->snap_vel, c->capacity)))
+            return rc;
+    }
+    if (c->n) {
+        SPHX_CUDA(cudaMemcpyAsync(c->snap_pos, c->b.pos4, c->n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
+        SPHX_CUDA(cudaMemcpyAsync(c->snap_vel, c->b.vel4, c->n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
+    }
+    return SPHX_OK;
+}
+
+int sphx_restore(sphx_ctx* c) {
+    int rc = enter(c);
+    if (rc) return rc;
+    if (!c->snap_pos) return SPHX_ERR_NOT_READY;
+    if (c->n) {
+        SPHX_CUDA(cudaMemcpyAsync(c->b.pos4, c->snap_pos, c->n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
+        SPHX_CUDA(cudaMemcpyAsync(c->b.vel4, c->snap_vel, c->n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
+    }
+    return SPHX_OK;
+}
+
+int sphx_debug_pairs(sphx_ctx* c, int64_t* counts, int64_t* idx, size_t* total_inout) {
+    int rc = enter(c);
+    if (rc) return rc;
+    if (!counts || !total_inout) return SPHX_ERR_INVALID_ARG;
+    if (!c->have_params) return SPHX_ERR_NOT_READY;
+    const size_t n = c->n;
+    if (n == 0) {
+        *total_inout = 0;
+        return SPHX_OK;
+    }
+    fill_step_const(c);
+    c->have_fields = false;  // the grid rebuild below replaces the sorted permutation
+    launch_begin_step(c->L, c->ds, 1);
+    launch_build_grid(c->L, c->sc, c->b, c->ds);
+    uint32_t* d_cnt = nullptr;
+    if ((rc = dmalloc(&d_cnt, n))) return rc;
+    launch_pair_counts(c->L, c->sc, c->b, c->ds, d_cnt);
+    std::vector<uint32_t> h_cnt(n);
+    cudaError_t e = cudaMemcpyAsync(h_cnt.data(), d_cnt, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d_cnt);
+    if (e != cudaSuccess) return cuda_fail(e);
+    rc = sync_status(c);
+    if (rc) return rc;
+    std::vector<uint64_t> off(n);
+    uint64_t total = 0;
+    for (size_t i = 0; i < n; ++i) {
+        counts[i] = h_cnt[i];
+        off[i] = total;
+        total += h_cnt[i];
+    }
+    const size_t cap = *total_inout;
+    *total_inout = (size_t)total;
+    if (!idx) return SPHX_OK;
+    if (cap < total) return SPHX_ERR_OVERFLOW;
+    uint64_t* d_off = nullptr;
+    int64_t* d_out = nullptr;
+    if ((rc = dmalloc(&d_off, n))) return rc;
+    if ((rc = dmalloc(&d_out, total))) {
+        cudaFree(d_off);
+        return rc;
+    }
+    e = cudaMemcpyAsync(d_off, off.data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) {
+        launch_pair_fill(c->L, c->sc, c->b, c->ds, d_off, d_out);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(idx, d_out, total * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d_off);
+    cudaFree(d_out);
+    if (e != cudaSuccess) return cuda_fail(e);
+    return SPHX_OK;
+}
+
+}  // extern "C"

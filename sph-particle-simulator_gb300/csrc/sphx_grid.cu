@@ -1,0 +1,336 @@
+// Grid build of one step (the GPU form of SpatialHash::build, spatial_hash.cpp:15-25),
+// the CFL timestep (SPHEngine::compute_cfl_timestep, sph_engine.cpp:312-333), the FP64
+// diagnostics and the host<->device packing kernels.
+//
+// Cells are the reference's own: floor(x * inv_cell) per axis with
+// inv_cell = 1.0f / neighbor_search_radius (spatial_hash.h:30-36, 63-66).  Instead of a
+// hash map of index vectors the occupied-cell box is laid out as a dense grid with a
+// linear key ((cx * dy + cy) * dz + cz), the keys are radix-sorted stably from insertion
+// order, and off[c] holds the first sorted position of cell c.  z is the fastest axis, so
+// the three cells (cx+dx, cy+dy, cz-1..cz+1) of one stencil row are one contiguous range
+// of the sorted arrays.  Particles with a NaN/inf coordinate get key == ncells: they sort
+// last and are never anyone's neighbour (every distance test with them fails in the
+// reference too).
+#include "sphx_internal.cuh"
+
+namespace sphx {
+
+static inline int grid_blocks(const LaunchCtx& L, int n, int threads, int per_sm = 4) {
+    const int need = (n + threads - 1) / threads;
+    const int cap = L.num_sms * per_sm;
+    return need < 1 ? 1 : (need < cap ? need : cap);
+}
+
+__global__ void k_begin_step(DevState* ds, int reset_bbox) {
+    if (threadIdx.x != 0) return;
+    ds->status = 0;
+    if (reset_bbox) {
+        for (int a = 0; a < 3; ++a) {
+            ds->cmin[a] = 0x7fffffff;
+            ds->cmax[a] = -0x7fffffff - 1;
+        }
+    }
+    ds->nonfinite = 0;
+    ds->vmax_bits = 0;
+    ds->occupied = 0;
+    ds->max_occ = 0;
+    ds->n_tiles = 0;
+}
+
+int launch_begin_step(const LaunchCtx& L, DevState* ds, int reset_bbox) {
+    k_begin_step<<<1, 32, 0, L.stream>>>(ds, reset_bbox);
+    return 1;
+}
+
+// ---- CFL ------------------------------------------------------------------------------
+
+// max |v_i| over the particles, NaN lengths ignored: std::max(m, v) keeps m when v is NaN
+// (sph_engine.cpp:316-322).  Non-negative floats order like their bit patterns.
+__global__ void k_vmax(const float4* __restrict__ vel4, int n, DevState* ds) {
+    uint32_t m = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 v = vel4[i];
+        const float len = xsqrt(xdot3(v.x, v.y, v.z));
+        if (!isnan(len)) m = max(m, __float_as_uint(len));
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(&ds->vmax_bits, m);
+}
+
+// dt = min({dt_cfl, dt_force, timestep}) with std::min's first-smallest rule; then
+// current_time_ += dt.
+__global__ void k_set_dt(StepConst c, DevState* ds, float host_dt) {
+    if (threadIdx.x != 0) return;
+    float dt = host_dt;  // a NaN dt is used as given, like SPHEngine::step (cpp:99-101)
+    if (host_dt <= 0.0f) {
+        const float vmax = __uint_as_float(ds->vmax_bits);
+        const float dt_cfl = xdiv(xmul(c.cfl, c.h), xadd(vmax, 1e-6f));
+        const float alen = xsqrt(xdot3(ds->a0[0], ds->a0[1], ds->a0[2]));
+        const float dt_force = xmul(c.cfl, xsqrt(xdiv(c.h, xadd(alen, 1e-6f))));
+        dt = dt_cfl;
+        if (dt_force < dt) dt = dt_force;
+        if (c.timestep < dt) dt = c.timestep;
+    }
+    ds->dt = dt;
+    ds->time = xadd(ds->time, dt);
+}
+
+int launch_cfl(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds,
+               float host_dt) {
+    int launches = 1;
+    if (host_dt <= 0.0f) {
+        k_vmax<<<grid_blocks(L, c.n, 256), 256, 0, L.stream>>>(b.vel4, c.n, ds);
+        ++launches;
+    }
+    k_set_dt<<<1, 32, 0, L.stream>>>(c, ds, host_dt);
+    return launches;
+}
+
+// ---- grid -----------------------------------------------------------------------------
+
+__global__ void k_bbox(const float4* __restrict__ pos4, int n, float inv_cell, DevState* ds) {
+    int mn[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff};
+    int mx[3] = {-0x7fffffff - 1, -0x7fffffff - 1, -0x7fffffff - 1};
+    uint32_t bad = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 p = pos4[i];
+        if (!finite3(p.x, p.y, p.z)) {
+            ++bad;
+            continue;
+        }
+        const int c[3] = {cell_coord(p.x, inv_cell), cell_coord(p.y, inv_cell),
+                          cell_coord(p.z, inv_cell)};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = min(mn[a], c[a]);
+            mx[a] = max(mx[a], c[a]);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = min(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+            mx[a] = max(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+        }
+        bad += __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            if (mn[a] != 0x7fffffff) atomicMin(&ds->cmin[a], mn[a]);
+            if (mx[a] != -0x7fffffff - 1) atomicMax(&ds->cmax[a], mx[a]);
+        }
+        if (bad) atomicAdd(&ds->nonfinite, bad);
+    }
+}
+
+__global__ void k_grid_setup(int n, uint32_t max_cells, DevState* ds) {
+    if (threadIdx.x != 0) return;
+    if ((int)ds->nonfinite >= n) {  // no finite particle: a one-cell grid, all keys sentinel
+        for (int a = 0; a < 3; ++a) {
+            ds->cmin[a] = 0;
+            ds->cmax[a] = 0;
+        }
+    }
+    unsigned long long cells = 1;
+    for (int a = 0; a < 3; ++a) {
+        const long long d = (long long)ds->cmax[a] - (long long)ds->cmin[a] + 1;
+        ds->dim[a] = (int)(d < 0x7fffffff ? d : 0x7fffffff);
+        cells = (d > (long long)max_cells) ? (unsigned long long)max_cells + 1
+                                           : cells * (unsigned long long)d;
+        if (cells > (unsigned long long)max_cells) cells = (unsigned long long)max_cells + 1;
+    }
+    if (cells > (unsigned long long)max_cells) {
+        ds->status = SPHX_ERR_DOMAIN;
+        ds->ncells = 0;
+        ds->passes = 0;
+        return;
+    }
+    ds->ncells = (uint32_t)cells;
+    const int bits = 32 - __clz(ds->ncells);  // key range is [0, ncells]
+    ds->passes = (uint32_t)((bits + kRadixBits - 1) / kRadixBits);
+}
+
+__global__ void k_keys(const float4* __restrict__ pos4, int n, float inv_cell,
+                       const DevState* ds, uint32_t* __restrict__ keys) {
+    if (ds->status) return;
+    const int cx0 = ds->cmin[0], cy0 = ds->cmin[1], cz0 = ds->cmin[2];
+    const uint32_t dy = ds->dim[1], dz = ds->dim[2], nc = ds->ncells;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 p = pos4[i];
+        uint32_t key = nc;
+        if (finite3(p.x, p.y, p.z)) {
+            const uint32_t x = (uint32_t)(cell_coord(p.x, inv_cell) - cx0);
+            const uint32_t y = (uint32_t)(cell_coord(p.y, inv_cell) - cy0);
+            const uint32_t z = (uint32_t)(cell_coord(p.z, inv_cell) - cz0);
+            key = (x * dy + y) * dz + z;
+        }
+        keys[i] = key;
+    }
+}
+
+// Gathers the state into cell-sorted order and keeps the sorted keys and permutation.
+__global__ void k_reorder(const Buffers b, int n, DevState* ds) {
+    if (ds->status) return;
+    const int sel = ds->passes & 1;
+    const uint32_t* __restrict__ ks = b.key[sel];
+    const uint32_t* __restrict__ vs = b.val[sel];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        uint32_t id = vs[k];
+        if (id >= (uint32_t)n) {  // never for a valid permutation: record, do not fault
+            atomicExch(&ds->status, SPHX_ERR_CUDA);
+            id = 0;
+        }
+        b.key_s[k] = ks[k];
+        b.id_s[k] = id;
+        b.pos4_s[k] = b.pos4[id];
+        b.vel4_s[k] = b.vel4[id];
+    }
+}
+
+// off[c] = first sorted position whose key is >= c, for c in [0, ncells + 1];
+// off[ncells] is the number of finite particles and off[ncells + 1] == n.
+__global__ void k_offsets(const uint32_t* __restrict__ key_s, int n, const DevState* ds,
+                          uint32_t* __restrict__ off) {
+    if (ds->status) return;
+    const uint32_t nc = ds->ncells;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= n; k += gridDim.x * blockDim.x) {
+        const uint32_t lo = (k == 0) ? 0u : key_s[k - 1] + 1u;
+        const uint32_t hi = (k == n) ? nc + 1u : key_s[k];
+        for (uint32_t c = lo; c <= hi; ++c) off[c] = (uint32_t)k;
+    }
+}
+
+int launch_build_grid(const LaunchCtx& L, const StepConst& c, const Buffers& b,
+                      DevState* ds) {
+    const int n = c.n;
+    const int gb = grid_blocks(L, n, 256);
+    k_bbox<<<gb, 256, 0, L.stream>>>(b.pos4, n, c.inv_cell, ds);
+    k_grid_setup<<<1, 32, 0, L.stream>>>(n, c.max_cells, ds);
+    k_keys<<<gb, 256, 0, L.stream>>>(b.pos4, n, c.inv_cell, ds, b.key[0]);
+    const int r = launch_radix_sort(L, b, ds, n);
+    k_reorder<<<grid_blocks(L, n, 256, 8), 256, 0, L.stream>>>(b, n, ds);
+    k_offsets<<<grid_blocks(L, n + 1, 256, 8), 256, 0, L.stream>>>(b.key_s, n, ds, b.off);
+    return 5 + r + launch_tile_scan(L, b, ds, n);
+}
+
+// ---- FP64 diagnostics of the state after a step -----------------------------------------
+// sums: mass, momentum x/y/z, kinetic energy, potential energy (-m g y), density.
+// Fixed partition and fixed-order final sum: bit-reproducible run to run.
+__global__ void __launch_bounds__(kDiagThreads) k_diag_partial(
+    const float4* __restrict__ pos4, const float4* __restrict__ vel4,
+    const float4* __restrict__ aux4_s, int n, float grav, double* __restrict__ part) {
+    double s[7] = {0, 0, 0, 0, 0, 0, 0};
+    const int per = (n + gridDim.x - 1) / gridDim.x;
+    const int i0 = blockIdx.x * per, i1 = min(n, i0 + per);
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const float4 p = pos4[i];
+        const float4 v = vel4[i];
+        const double m = p.w;
+        s[0] += m;
+        s[1] += m * v.x;
+        s[2] += m * v.y;
+        s[3] += m * v.z;
+        s[4] += 0.5 * m * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
+        s[5] += -m * (double)grav * (double)p.y;
+        s[6] += (double)aux4_s[i].x;
+    }
+    __shared__ double red[kDiagThreads / 32][7];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+        double v = s[k];
+#pragma unroll
+        for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 7) {
+        double v = 0;
+        for (int w = 0; w < kDiagThreads / 32; ++w) v += red[w][threadIdx.x];
+        part[blockIdx.x * kDiagSums + threadIdx.x] = v;
+    }
+}
+
+__global__ void k_diag_final(const double* __restrict__ part, int nb, DevState* ds) {
+    if (threadIdx.x >= 7) return;
+    double v = 0;
+    for (int b = 0; b < nb; ++b) v += part[b * kDiagSums + threadIdx.x];
+    ds->sums[threadIdx.x] = v;
+}
+
+int launch_diag(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds) {
+    k_diag_partial<<<b.diag_blocks, kDiagThreads, 0, L.stream>>>(b.pos4, b.vel4, b.aux4_s, c.n,
+                                                                 c.grav, b.diag_part);
+    k_diag_final<<<1, 32, 0, L.stream>>>(b.diag_part, b.diag_blocks, ds);
+    return 2;
+}
+
+// ---- packing ----------------------------------------------------------------------------
+
+__global__ void k_pack(int n, const float* __restrict__ pos3, const float* __restrict__ vel3,
+                       const float* __restrict__ mass, float4* __restrict__ pos4,
+                       float4* __restrict__ vel4) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        pos4[i] = make_float4(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2], mass[i]);
+        vel4[i] = vel3 ? make_float4(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2], 0.0f)
+                       : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+}
+
+void launch_pack(const LaunchCtx& L, int n, const float* pos3, const float* vel3,
+                 const float* mass, float4* pos4, float4* vel4) {
+    k_pack<<<grid_blocks(L, n, 256, 8), 256, 0, L.stream>>>(n, pos3, vel3, mass, pos4, vel4);
+}
+
+__global__ void k_unpack_state(int n, const float4* __restrict__ pos4,
+                               const float4* __restrict__ vel4, float* __restrict__ pos3,
+                               float* __restrict__ vel3) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (pos3) {
+            const float4 p = pos4[i];
+            pos3[3 * i] = p.x;
+            pos3[3 * i + 1] = p.y;
+            pos3[3 * i + 2] = p.z;
+        }
+        if (vel3) {
+            const float4 v = vel4[i];
+            vel3[3 * i] = v.x;
+            vel3[3 * i + 1] = v.y;
+            vel3[3 * i + 2] = v.z;
+        }
+    }
+}
+
+void launch_unpack_state(const LaunchCtx& L, int n, const float4* pos4, const float4* vel4,
+                         float* pos3, float* vel3) {
+    k_unpack_state<<<grid_blocks(L, n, 256, 8), 256, 0, L.stream>>>(n, pos4, vel4, pos3, vel3);
+}
+
+__global__ void k_unpack_sorted(int n, const uint32_t* __restrict__ id_s,
+                                const float4* __restrict__ aux4_s,
+                                const float4* __restrict__ acc4_s, float* __restrict__ rho,
+                                float* __restrict__ pressure, float* __restrict__ acc3) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const uint32_t id = id_s[k];
+        const float4 a = aux4_s[k];
+        if (rho) rho[id] = a.x;
+        if (pressure) pressure[id] = a.y;
+        if (acc3) {
+            const float4 g = acc4_s[k];
+            acc3[3 * id] = g.x;
+            acc3[3 * id + 1] = g.y;
+            acc3[3 * id + 2] = g.z;
+        }
+    }
+}
+
+void launch_unpack_sorted(const LaunchCtx& L, int n, const uint32_t* id_s, const float4* aux4_s,
+                          const float4* acc4_s, float* rho, float* pressure, float* acc3) {
+    k_unpack_sorted<<<grid_blocks(L, n, 256, 8), 256, 0, L.stream>>>(n, id_s, aux4_s, acc4_s,
+                                                                     rho, pressure, acc3);
+}
+
+}  // namespace sphx

@@ -1,0 +1,181 @@
+// Internal declarations of the sm_103a SPH step: device-resident state, per-step
+// constants, exact-arithmetic helpers and the launch wrappers shared by the .cu files.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sphx.h"
+
+namespace sphx {
+
+constexpr int kWarp = 32;
+constexpr int kTile = 32;              // particles of one cell handled by one warp
+constexpr int kRadixBits = 8;
+constexpr int kRadixBuckets = 1 << kRadixBits;
+constexpr int kRadixThreads = 256;
+constexpr int kRadixItems = 16;
+constexpr int kRadixTileN = kRadixThreads * kRadixItems;  // keys per radix block
+constexpr int kMaxPasses = 4;                             // 32-bit keys
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTileN = kScanThreads * kScanItems;
+constexpr int kDiagThreads = 256;
+constexpr int kDiagSums = 8;
+constexpr int kCellClamp = 1 << 30;    // |cell coordinate| clamp for finite positions
+
+// Constants of one step, computed on the host in float exactly as the reference does
+// (SpatialHash::set_cell_size, spatial_hash.h:63-66; CubicSplineKernel ctor,
+// kernels.cpp:12-14, 23-36) and passed to the kernels by value.
+struct StepConst {
+    int n;                 // particles loaded
+    float inv_cell;        // 1.0f / neighbor_search_radius
+    float r2;              // neighbor_search_radius * neighbor_search_radius
+    float h, h_sq, sigma;  // kernel constants
+    float w0;              // W(vec3(0)) -- the self term factor
+    float rest, gas, visc, grav, damping, cfl, timestep;
+    float lo[3], hi[3];    // box
+    uint32_t max_cells;    // capacity of the dense cell grid
+};
+
+// Device-resident scalars written and read by the kernels of a step.
+struct DevState {
+    int status;                 // 0 or SPHX_ERR_* raised on the device
+    int cmin[3], cmax[3];       // box of occupied cells (finite particles)
+    int dim[3];                 // grid extent in cells
+    uint32_t ncells;            // dim product; also the key of non-finite particles
+    uint32_t passes;            // radix passes needed this step
+    uint32_t n_tiles;           // warp work items
+    uint32_t nonfinite;         // particles with a NaN/inf coordinate
+    uint32_t vmax_bits;         // max |v| (float bits) for the CFL rule
+    uint32_t occupied;          // occupied cells
+    uint32_t max_occ;           // particles in the fullest cell
+    uint32_t pad0;
+    float dt;                   // dt of the current step
+    float time;                 // current_time_
+    float a0[4];                // accelerations_[0] (persists across steps)
+    unsigned long long max_nn;  // max |N(i)| since the last stats reset
+    double sums[kDiagSums];     // FP64 diagnostics of the state after the last step
+};
+
+struct Buffers {
+    float4* pos4;     // insertion order: x, y, z, mass
+    float4* vel4;     // insertion order: vx, vy, vz, 0
+    float4* pos4_s;   // cell-sorted copies
+    float4* vel4_s;
+    float4* aux4_s;   // cell-sorted: rho, P, 2*rho, mass/rho
+    float4* acc4_s;   // cell-sorted accelerations of the last step/eval
+    uint32_t* key[2]; // radix ping-pong
+    uint32_t* val[2];
+    uint32_t* key_s;  // sorted cell keys
+    uint32_t* id_s;   // sorted position -> insertion index
+    uint32_t* off;    // dense cell grid: first sorted position of each cell (max_cells + 2)
+    uint32_t* tile_start;
+    uint32_t* hist;   // radix histograms / offsets
+    uint32_t* scan_part;
+    double* diag_part;
+    int radix_blocks;
+    int scan_part_cap;
+    int diag_blocks;
+};
+
+// ---- exact float arithmetic: IEEE round-to-nearest, never contracted into FMA ---------
+__device__ __forceinline__ float xmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float xadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float xsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float xdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float xsqrt(float a) { return __fsqrt_rn(a); }
+
+// glm::dot(v, v) = (x*x + y*y) + z*z (products rounded first)
+__device__ __forceinline__ float xdot3(float x, float y, float z) {
+    return xadd(xadd(xmul(x, x), xmul(y, y)), xmul(z, z));
+}
+
+// float(2)/float(3) and float(1)/float(6), the constants the reference folds at compile
+// time in W_3d (kernels.cpp:58-66)
+constexpr float kTwoThirds = 0x1.555556p-1f;
+constexpr float kOneSixth = 0x1.555556p-3f;
+
+// CubicSplineKernel::W_3d (kernels.cpp:58-66)
+__device__ __forceinline__ float cubic_w(const StepConst& c, float q) {
+    if (q >= 0.0f && q <= 1.0f) {
+        const float t = xadd(xsub(kTwoThirds, xmul(q, q)), xmul(xmul(xmul(0.5f, q), q), q));
+        return xmul(c.sigma, t);
+    } else if (q > 1.0f && q <= 2.0f) {
+        const float tmp = xsub(2.0f, q);
+        return xmul(c.sigma, xmul(xmul(xmul(kOneSixth, tmp), tmp), tmp));
+    }
+    return 0.0f;
+}
+
+// scalar factor of CubicSplineKernel::gradW_3d (kernels.cpp:96-108):
+// grad = factor * (r / |r|) / h ; r_len >= 1e-6 is the caller's business
+__device__ __forceinline__ float cubic_grad_factor(const StepConst& c, float q) {
+    if (q >= 0.0f && q <= 1.0f) {
+        return xmul(c.sigma, xadd(xmul(-2.0f, q), xmul(xmul(1.5f, q), q)));
+    } else if (q > 1.0f && q <= 2.0f) {
+        const float tmp = xsub(2.0f, q);
+        return xmul(-c.sigma, xmul(xmul(0.5f, tmp), tmp));
+    }
+    return 0.0f;
+}
+
+// CubicSplineKernel::laplacianW_3d (kernels.cpp:130-138)
+__device__ __forceinline__ float cubic_lap(const StepConst& c, float q) {
+    if (q >= 0.0f && q <= 1.0f) {
+        return xdiv(xmul(c.sigma, xadd(-2.0f, xmul(3.0f, q))), c.h_sq);
+    } else if (q > 1.0f && q <= 2.0f) {
+        const float tmp = xsub(2.0f, q);
+        return xdiv(xmul(c.sigma, tmp), c.h_sq);
+    }
+    return 0.0f;
+}
+
+__device__ __forceinline__ bool finite3(float x, float y, float z) {
+    return isfinite(x) && isfinite(y) && isfinite(z);
+}
+
+// Cell coordinate of one axis: floor(x * inv_cell) as SpatialHash::get_grid_coords
+// computes it (spatial_hash.h:30-36), clamped to +-2^30 so that every finite position
+// has a well-defined cell (clamping keeps neighbouring cells neighbouring).
+__device__ __forceinline__ int cell_coord(float x, float inv_cell) {
+    float f = floorf(xmul(x, inv_cell));
+    f = fminf(fmaxf(f, -(float)kCellClamp), (float)(kCellClamp - 1));
+    return (int)f;
+}
+
+// ---- launch wrappers (host) --------------------------------------------------------
+struct LaunchCtx {
+    cudaStream_t stream;
+    int num_sms;
+    int warps_per_block;
+    int blocks_per_sm;
+};
+
+int launch_begin_step(const LaunchCtx& L, DevState* ds, int reset_bbox);
+int launch_cfl(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds,
+                float host_dt);
+int launch_build_grid(const LaunchCtx& L, const StepConst& c, const Buffers& b,
+                       DevState* ds);
+int launch_density(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds);
+int launch_force(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds,
+                  int integrate);
+int launch_diag(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds);
+void launch_pair_counts(const LaunchCtx& L, const StepConst& c, const Buffers& b,
+                        DevState* ds, uint32_t* counts_by_id);
+void launch_pair_fill(const LaunchCtx& L, const StepConst& c, const Buffers& b,
+                      DevState* ds, const uint64_t* offsets_by_id, int64_t* out_idx);
+
+// radix sort + scan (sphx_sort.cu)
+int launch_radix_sort(const LaunchCtx& L, const Buffers& b, DevState* ds, int n);
+int launch_tile_scan(const LaunchCtx& L, const Buffers& b, DevState* ds, int n);
+
+// io (sphx_grid.cu)
+void launch_pack(const LaunchCtx& L, int n, const float* pos3, const float* vel3,
+                 const float* mass, float4* pos4, float4* vel4);
+void launch_unpack_state(const LaunchCtx& L, int n, const float4* pos4, const float4* vel4,
+                         float* pos3, float* vel3);
+void launch_unpack_sorted(const LaunchCtx& L, int n, const uint32_t* id_s,
+                          const float4* aux4_s, const float4* acc4_s, float* rho,
+                          float* pressure, float* acc3);
+
+}  // namespace sphx

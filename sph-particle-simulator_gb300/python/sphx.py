@@ -1,0 +1,256 @@
+"""ctypes binding of the sphx C ABI (include/sphx.h).
+
+This is how Python callers -- the tests, the bench and the smoke check -- drive the GPU
+step through exactly the entry points a C/C++ host binds.  The shared library is the
+in-tree build <package>/lib/libsphx.so; if it is missing the import fails loudly: there is
+no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parents[1]
+LIB_PATH = Path(os.environ.get("SPHX_LIB", _PKG / "lib" / "libsphx.so"))
+
+OK = 0
+ERRORS = {
+    -1: "SPHX_ERR_INVALID_ARG", -2: "SPHX_ERR_OOM", -3: "SPHX_ERR_CUDA",
+    -4: "SPHX_ERR_TIMEOUT", -5: "SPHX_ERR_CAPACITY", -6: "SPHX_ERR_NOT_READY",
+    -7: "SPHX_ERR_DOMAIN", -8: "SPHX_ERR_OVERFLOW",
+}
+MODE_EXACT = 0
+
+# every symbol include/sphx.h declares
+EXPORTS = (
+    "sphx_version", "sphx_strerror", "sphx_create", "sphx_destroy", "sphx_set_stream",
+    "sphx_set_params", "sphx_upload", "sphx_step", "sphx_eval", "sphx_download",
+    "sphx_size", "sphx_get_time", "sphx_set_time", "sphx_get_stats", "sphx_reset_stats",
+    "sphx_snapshot", "sphx_restore", "sphx_debug_pairs",
+)
+
+
+class SphxParams(C.Structure):
+    _fields_ = [(n, C.c_float) for n in (
+        "rest_density", "gas_constant", "viscosity", "smoothing_length", "particle_mass",
+        "timestep", "gravity", "damping", "cfl_factor", "xmin", "xmax", "ymin", "ymax",
+        "zmin", "zmax", "neighbor_search_radius")]
+
+
+class SphxTuning(C.Structure):
+    _fields_ = [("mode", C.c_int), ("warps_per_block", C.c_int), ("blocks_per_sm", C.c_int),
+                ("max_grid_cells", C.c_int64), ("profile", C.c_int)]
+
+
+class SphxStats(C.Structure):
+    _fields_ = [
+        ("total_time", C.c_double), ("neighbor_search_time", C.c_double),
+        ("density_computation_time", C.c_double), ("force_computation_time", C.c_double),
+        ("integration_time", C.c_double), ("max_neighbors", C.c_uint64),
+        ("total_neighbor_queries", C.c_uint64), ("steps", C.c_uint64),
+        ("current_time", C.c_float), ("last_dt", C.c_float),
+        ("occupied_cells", C.c_uint32), ("max_cell_occupancy", C.c_uint32),
+        ("nonfinite_particles", C.c_uint32), ("grid_cells", C.c_uint32),
+        ("sum_mass", C.c_double), ("momentum", C.c_double * 3),
+        ("kinetic_energy", C.c_double), ("potential_energy", C.c_double),
+        ("sum_density", C.c_double), ("kernel_launches", C.c_uint64),
+    ]
+
+    def as_dict(self) -> dict:
+        d = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            d[name] = list(v) if name == "momentum" else v
+        return d
+
+
+class SphxError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        super().__init__(f"{where}: {ERRORS.get(code, code)} ({code})")
+        self.code = code
+
+
+def load_library(path: Path | str = LIB_PATH) -> C.CDLL:
+    path = Path(path)
+    if not path.exists():
+        raise ImportError(f"sphx CUDA library not built: {path} (run __graft_entry__.build())")
+    lib = C.CDLL(str(path))
+    vp, sz, fp = C.c_void_p, C.c_size_t, C.c_void_p
+    sig = {
+        "sphx_version": ([], C.c_int),
+        "sphx_strerror": ([C.c_int], C.c_char_p),
+        "sphx_create": ([C.POINTER(vp), sz, C.POINTER(SphxTuning)], C.c_int),
+        "sphx_destroy": ([vp], None),
+        "sphx_set_stream": ([vp, vp], C.c_int),
+        "sphx_set_params": ([vp, C.POINTER(SphxParams)], C.c_int),
+        "sphx_upload": ([vp, sz, fp, fp, fp], C.c_int),
+        "sphx_step": ([vp, C.c_float], C.c_int),
+        "sphx_eval": ([vp], C.c_int),
+        "sphx_download": ([vp, fp, fp, fp, fp, fp], C.c_int),
+        "sphx_size": ([vp, C.POINTER(sz)], C.c_int),
+        "sphx_get_time": ([vp, C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
+        "sphx_set_time": ([vp, C.c_float], C.c_int),
+        "sphx_get_stats": ([vp, C.POINTER(SphxStats)], C.c_int),
+        "sphx_reset_stats": ([vp], C.c_int),
+        "sphx_snapshot": ([vp], C.c_int),
+        "sphx_restore": ([vp], C.c_int),
+        "sphx_debug_pairs": ([vp, fp, fp, C.POINTER(sz)], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    return lib
+
+
+_LIB: C.CDLL | None = None
+
+
+def lib() -> C.CDLL:
+    global _LIB
+    if _LIB is None:
+        _LIB = load_library()
+    return _LIB
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f32(a, shape_last=None) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a
+
+
+def params_struct(p16) -> SphxParams:
+    p = np.asarray(p16, dtype=np.float32).ravel()
+    if p.size != 16:
+        raise ValueError("a parameter block has 16 floats")
+    return SphxParams(*[float(x) for x in p])
+
+
+class Context:
+    """One sphx context (one GPU step engine)."""
+
+    def __init__(self, capacity: int, *, mode: int = MODE_EXACT, warps_per_block: int = 0,
+                 blocks_per_sm: int = 0, max_grid_cells: int = 0, profile: bool = False):
+        self._lib = lib()
+        self._h = C.c_void_p()
+        t = SphxTuning(mode, warps_per_block, blocks_per_sm, max_grid_cells, int(profile))
+        self._check(self._lib.sphx_create(C.byref(self._h), capacity, C.byref(t)), "sphx_create")
+        self.capacity = capacity
+
+    def _check(self, rc: int, where: str):
+        if rc != OK:
+            raise SphxError(rc, where)
+
+    def close(self):
+        if self._h:
+            self._lib.sphx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_stream(self, stream_ptr: int | None):
+        self._check(self._lib.sphx_set_stream(self._h, stream_ptr or None), "sphx_set_stream")
+
+    def set_params(self, p16):
+        self._check(self._lib.sphx_set_params(self._h, C.byref(params_struct(p16))),
+                    "sphx_set_params")
+
+    def upload(self, pos, vel=None, mass=None):
+        pos = _f32(pos).reshape(-1, 3)
+        n = pos.shape[0]
+        vel = None if vel is None else _f32(vel).reshape(n, 3)
+        mass = _f32(mass).reshape(n)
+        self._keep = (pos, vel, mass)
+        self._check(self._lib.sphx_upload(self._h, n, _ptr(pos), _ptr(vel), _ptr(mass)),
+                    "sphx_upload")
+
+    def upload_ptr(self, n: int, pos_ptr: int, vel_ptr: int | None, mass_ptr: int):
+        """Upload from raw host pointers (e.g. pinned buffers)."""
+        self._check(self._lib.sphx_upload(self._h, n, C.c_void_p(pos_ptr),
+                                          C.c_void_p(vel_ptr) if vel_ptr else None,
+                                          C.c_void_p(mass_ptr)), "sphx_upload")
+
+    def step(self, dt: float = 0.0):
+        self._check(self._lib.sphx_step(self._h, C.c_float(dt)), "sphx_step")
+
+    def eval(self):
+        self._check(self._lib.sphx_eval(self._h), "sphx_eval")
+
+    def size(self) -> int:
+        n = C.c_size_t()
+        self._check(self._lib.sphx_size(self._h, C.byref(n)), "sphx_size")
+        return n.value
+
+    def download(self, pos=True, vel=True, rho=True, pressure=True, acc=True) -> dict:
+        n = self.size()
+        out = {}
+        if pos:
+            out["pos"] = np.empty((n, 3), np.float32)
+        if vel:
+            out["vel"] = np.empty((n, 3), np.float32)
+        if rho:
+            out["rho"] = np.empty(n, np.float32)
+        if pressure:
+            out["pressure"] = np.empty(n, np.float32)
+        if acc:
+            out["acc"] = np.empty((n, 3), np.float32)
+        self._check(self._lib.sphx_download(
+            self._h, _ptr(out.get("pos")), _ptr(out.get("vel")), _ptr(out.get("rho")),
+            _ptr(out.get("pressure")), _ptr(out.get("acc"))), "sphx_download")
+        return out
+
+    def download_ptr(self, pos_ptr, vel_ptr, rho_ptr, p_ptr, acc_ptr):
+        cv = lambda p: C.c_void_p(p) if p else None
+        self._check(self._lib.sphx_download(self._h, cv(pos_ptr), cv(vel_ptr), cv(rho_ptr),
+                                            cv(p_ptr), cv(acc_ptr)), "sphx_download")
+
+    def time(self) -> tuple[float, float]:
+        t, dt = C.c_float(), C.c_float()
+        self._check(self._lib.sphx_get_time(self._h, C.byref(t), C.byref(dt)), "sphx_get_time")
+        return t.value, dt.value
+
+    def set_time(self, t: float):
+        self._check(self._lib.sphx_set_time(self._h, C.c_float(t)), "sphx_set_time")
+
+    def stats(self) -> dict:
+        s = SphxStats()
+        self._check(self._lib.sphx_get_stats(self._h, C.byref(s)), "sphx_get_stats")
+        return s.as_dict()
+
+    def reset_stats(self):
+        self._check(self._lib.sphx_reset_stats(self._h), "sphx_reset_stats")
+
+    def snapshot(self):
+        self._check(self._lib.sphx_snapshot(self._h), "sphx_snapshot")
+
+    def restore(self):
+        self._check(self._lib.sphx_restore(self._h), "sphx_restore")
+
+    def pairs(self) -> tuple[np.ndarray, np.ndarray]:
+        """Neighbour lists of the current state: (counts[n], concatenated insertion ids)."""
+        n = self.size()
+        counts = np.zeros(n, np.int64)
+        total = C.c_size_t(0)
+        self._check(self._lib.sphx_debug_pairs(self._h, _ptr(counts), None, C.byref(total)),
+                    "sphx_debug_pairs")
+        idx = np.zeros(max(total.value, 1), np.int64)
+        total2 = C.c_size_t(total.value)
+        self._check(self._lib.sphx_debug_pairs(self._h, _ptr(counts), _ptr(idx),
+                                               C.byref(total2)), "sphx_debug_pairs")
+        return counts, idx[: total2.value]

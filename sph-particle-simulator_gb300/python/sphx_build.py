@@ -1,0 +1,110 @@
+"""Build recipe for the sm_103a SPH step library and its host-side companions.
+
+  libsphx.so        CUDA kernels + C ABI (include/sphx.h)        -> <pkg>/lib/
+  libsph_gb300.so   C++17 drop-in SPHEngine over the C ABI       -> <pkg>/lib/
+  sph*.so           pybind11 module `sph` over the drop-in       -> <pkg>/lib/
+  oracle (tests)    oracle/_build/libsph_oracle.so, and oracle/_ref/libsph_ref.so when the
+                    reference sources are present (oracle/build_ref.sh)
+
+Every translation unit is compiled in parallel with one -gencode (sm_103a); host code is
+built with -ffp-contract=off so float expressions round exactly as written.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+import sysconfig
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parents[1]
+REPO = PKG.parent
+LIB = PKG / "lib"
+OBJ = PKG / "_build"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
+              "-ffp-contract=off", "-Xptxas", "-warn-spills", f"-I{REPO / 'include'}"]
+CUDA_SOURCES = ["sphx_sort.cu", "sphx_grid.cu", "sphx_passes.cu", "sphx_capi.cu"]
+
+
+def _nvcc() -> str:
+    home = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    cand = Path(home) / "bin" / "nvcc"
+    return str(cand) if cand.exists() else (shutil.which("nvcc") or "nvcc")
+
+
+def _run_parallel(cmds: list[list[str]]) -> None:
+    procs = [(c, subprocess.Popen(c, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)) for c in cmds]
+    errors = []
+    for c, p in procs:
+        out, _ = p.communicate()
+        if p.returncode != 0:
+            errors.append(f"$ {' '.join(c)}\n{out.decode(errors='replace')}")
+        elif out.strip():
+            sys.stderr.write(out.decode(errors="replace"))
+    if errors:
+        raise RuntimeError("build failed:\n" + "\n".join(errors))
+
+
+def _stale(target: Path, deps: list[Path]) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(d.stat().st_mtime > t for d in deps)
+
+
+def build_sphx(force: bool = False) -> Path:
+    """Compiles the CUDA library; returns the .so path."""
+    LIB.mkdir(exist_ok=True)
+    OBJ.mkdir(exist_ok=True)
+    csrc = PKG / "csrc"
+    headers = list(csrc.glob("*.cuh")) + [REPO / "include" / "sphx.h"]
+    nvcc = _nvcc()
+    cmds, objs = [], []
+    for s in CUDA_SOURCES:
+        src, obj = csrc / s, OBJ / (Path(s).stem + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [src] + headers):
+            cmds.append([nvcc, *NVCC_FLAGS, *ARCH, "-c", str(src), "-o", str(obj)])
+    _run_parallel(cmds)
+    so = LIB / "libsphx.so"
+    if force or cmds or _stale(so, objs):
+        _run_parallel([[nvcc, "-shared", *ARCH, "-o", str(so), *map(str, objs)]])
+    return so
+
+
+def build_oracle(force: bool = False) -> Path:
+    """Compiles the C restatement of the reference step (test infrastructure)."""
+    out_dir = REPO / "oracle" / "_build"
+    out_dir.mkdir(exist_ok=True)
+    src = REPO / "oracle" / "sph_oracle.c"
+    so = out_dir / "libsph_oracle.so"
+    if force or _stale(so, [src, REPO / "oracle" / "sph_oracle.h"]):
+        _run_parallel([["gcc", "-std=c11", "-D_GNU_SOURCE", "-O2", "-fopenmp",
+                        "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+                        str(src), "-o", str(so), "-lm"]])
+    return so
+
+
+def build_ref() -> Path | None:
+    """Builds oracle/_ref from the reference sources when they are present."""
+    ref = Path(os.environ.get("SPH_REFERENCE_DIR", "/root/reference"))
+    if not (ref / "src" / "sph_engine.cpp").exists():
+        return None
+    so = REPO / "oracle" / "_ref" / "libsph_ref.so"
+    deps = [REPO / "oracle" / "ref_harness.cpp", REPO / "oracle" / "glm_shim" / "glm" / "glm.hpp"]
+    if _stale(so, deps):
+        subprocess.run(["bash", str(REPO / "oracle" / "build_ref.sh"), str(ref)], check=True,
+                       stdout=subprocess.DEVNULL)
+    return so
+
+
+def build_all(force: bool = False) -> dict:
+    out = {"sphx": build_sphx(force), "oracle": build_oracle(force)}
+    out["ref"] = build_ref()
+    return out
+
+
+if __name__ == "__main__":
+    print(build_all(force="--force" in sys.argv))

@@ -1,0 +1,117 @@
+"""Generates tests/golden/sph_ref_golden.npz from the reference's own code.
+
+Runs the reference SPH core compiled from its sources (oracle/_ref/libsph_ref.so, built by
+oracle/build_ref.sh from the reference checkout) on small seeded inputs and stores inputs
+and outputs as fixtures.  The fixtures travel with the repository; the reference checkout
+does not.  Re-run with:  python tests/golden/make_golden.py
+
+Cases (all arrays float32 unless noted, vectors as (n, 3)):
+  lattice     8x8x8 jittered lattice (spacing 0.01, jitter 5e-4, seed 7), box [0,1]^3
+  exact       6x6x6 lattice without jitter: exact ties |r| == r_search occur
+  edge        hand-made: coincident pairs, NaN / inf coordinates, a far particle, particles
+              outside the box, particles on cell faces, a zero-velocity-mass mix
+  collapse    12x12x12 jittered lattice stepped 4 times at dt 1e-3 (the reference's
+              dynamics degenerate after step 1: clamped walls, crowded cells)
+For each case: params16, pos, vel, mass; the neighbour lists of the initial state
+(counts int64, idx int32, reference order); rho/P/acc of one field evaluation; and for
+`steps` steps of SPHEngine::step(dt) (dt > 0 fixed, dt == 0 adaptive CFL) the positions,
+velocities, densities, pressures and current time after each step.
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(REPO / "sph-particle-simulator_gb300" / "python"))
+sys.path.insert(0, str(REPO / "oracle"))
+
+import sphx_inputs as I  # noqa: E402
+import sph_oracle as O  # noqa: E402
+
+
+def edge_case():
+    pts = [
+        (0.10, 0.10, 0.10), (0.10, 0.10, 0.10), (0.10, 0.10, 0.10),  # coincident triple
+        (0.12, 0.10, 0.10), (0.10, 0.13, 0.10), (0.10, 0.10, 0.14),  # at <= r and = r
+        (0.08, 0.08, 0.08),                                           # on a cell corner
+        (0.16, 0.12, 0.04), (0.04, 0.04, 0.04),                       # cell faces (r = 0.04)
+        (np.nan, 0.2, 0.2), (0.2, np.inf, 0.2), (-np.inf, 0.1, 0.1),  # non-finite
+        (0.30, 0.30, 0.30), (0.32, 0.31, 0.30), (0.30, 0.33, 0.31),
+        (1.5, 0.5, 0.5), (1.52, 0.5, 0.5),                            # outside the box
+        (-0.2, 0.5, 0.5),
+        (500.0, 500.0, 500.0), (500.01, 500.0, 500.0),                # far away
+        (0.5, 0.5, 0.5), (0.5 + 0.04, 0.5, 0.5), (0.5, 0.5 + 0.039999, 0.5),
+        (0.5, 0.5, 0.5 + 0.040001),
+    ]
+    rng = np.random.default_rng(11)
+    extra = (0.6 + rng.random((24, 3)) * 0.06).tolist()
+    pos = np.array(pts + extra, np.float32)
+    n = pos.shape[0]
+    vel = (rng.standard_normal((n, 3)) * 0.3).astype(np.float32)
+    vel[3] = (np.nan, 0.0, 0.0)
+    mass = np.full(n, 1e-3, np.float32)
+    mass[5] = 2e-3
+    prm = I.params16(xmin=0.0, xmax=1.0, ymin=0.0, ymax=1.0, zmin=0.0, zmax=1.0)
+    return pos, vel, mass, prm
+
+
+def cases():
+    box = dict(xmin=0.0, xmax=1.0, ymin=0.0, ymax=1.0, zmin=0.0, zmax=1.0)
+    pos = I.lattice(8, 8, 8, seed=7) + np.float32(0.2)
+    n = pos.shape[0]
+    yield "lattice", pos, np.zeros((n, 3), np.float32), np.full(n, 1e-3, np.float32), \
+        I.params16(**box), [1e-3, 1e-3, 0.0, 0.0]
+    pos = I.lattice(6, 6, 6, jitter=0.0)  # on cell faces, with exact ties
+    n = pos.shape[0]
+    yield "exact", pos, np.zeros((n, 3), np.float32), np.full(n, 1e-3, np.float32), \
+        I.params16(**box), [1e-3, 0.0]
+    p, v, m, prm = edge_case()
+    yield "edge", p, v, m, prm, [1e-3, 0.0, 1e-3]
+    pos = I.lattice(12, 12, 12, seed=9)
+    n = pos.shape[0]
+    yield "collapse", pos, np.zeros((n, 3), np.float32), np.full(n, 1e-3, np.float32), \
+        I.params16(**box), [1e-3, 1e-3, 1e-3, 1e-3]
+
+
+def main():
+    ref = O.Ref()
+    out = {}
+    for name, pos, vel, mass, prm, dts in cases():
+        n = pos.shape[0]
+        counts, idx = ref.query(pos, float(prm[15]))
+        rho, P, acc = ref.fields(pos, vel, mass, prm)
+        e = O.Engine(ref, n)
+        e.initialize(prm)
+        e.add(pos, vel, mass)
+        traj = []
+        for dt in dts:
+            e.step(dt)
+            g = e.get()
+            traj.append((g["pos"], g["vel"], g["rho"], g["pressure"], e.time()))
+        pre = f"{name}/"
+        out[pre + "params"] = prm
+        out[pre + "pos"] = pos
+        out[pre + "vel"] = vel
+        out[pre + "mass"] = mass
+        out[pre + "counts"] = counts
+        out[pre + "idx"] = idx.astype(np.int32)
+        out[pre + "rho"] = rho
+        out[pre + "pressure"] = P
+        out[pre + "acc"] = acc
+        out[pre + "dts"] = np.array(dts, np.float32)
+        out[pre + "traj_pos"] = np.stack([t[0] for t in traj])
+        out[pre + "traj_vel"] = np.stack([t[1] for t in traj])
+        out[pre + "traj_rho"] = np.stack([t[2] for t in traj])
+        out[pre + "traj_pressure"] = np.stack([t[3] for t in traj])
+        out[pre + "traj_time"] = np.array([t[4] for t in traj], np.float32)
+        print(f"{name}: n={n} pairs={idx.size} max|N|={counts.max()} steps={len(dts)}")
+    path = Path(__file__).with_name("sph_ref_golden.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({path.stat().st_size / 1024:.0f} KiB)")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,209 @@
+"""GPU step parity, through the C ABI, against the oracle.
+
+The oracle here is the C restatement of the reference step, itself pinned bit for bit to
+the reference's own code by tests/test_oracle.py and to the reference-generated fixtures
+in tests/golden/.  In SPHX_MODE_EXACT the GPU must reproduce every field bit for bit:
+neighbour lists in the reference's order, density, pressure, acceleration, and after a
+step position, velocity and time (NaN compares equal to NaN).
+"""
+import numpy as np
+import pytest
+
+import sph_oracle as O
+import sphx
+import sphx_inputs as I
+from conftest import GOLDEN_CASES, golden_case
+
+pytestmark = pytest.mark.gpu
+
+
+def make_ctx(n, params, pos, vel, mass, **kw):
+    ctx = sphx.Context(max(n, 1), **kw)
+    ctx.set_params(params)
+    ctx.upload(pos, vel, mass)
+    return ctx
+
+
+def assert_bits(a, b, name):
+    assert O.bits_equal(a, b), O.mismatch_report(a, b, name)
+
+
+# ---- against the reference-generated fixtures ----------------------------------------
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_gpu_neighbour_lists_match_reference_fixture(built, golden, case):
+    g = golden_case(golden, case)
+    ctx = make_ctx(g["pos"].shape[0], g["params"], g["pos"], g["vel"], g["mass"])
+    counts, idx = ctx.pairs()
+    assert np.array_equal(counts, g["counts"])
+    assert np.array_equal(idx, g["idx"].astype(np.int64))  # same order
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_gpu_fields_match_reference_fixture(built, golden, case):
+    g = golden_case(golden, case)
+    ctx = make_ctx(g["pos"].shape[0], g["params"], g["pos"], g["vel"], g["mass"])
+    ctx.eval()
+    out = ctx.download()
+    assert_bits(out["rho"], g["rho"], "rho")
+    assert_bits(out["pressure"], g["pressure"], "P")
+    assert_bits(out["acc"], g["acc"], "acc")
+    assert_bits(out["pos"], g["pos"], "pos unchanged by eval")
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_gpu_trajectory_matches_reference_fixture(built, golden, case):
+    g = golden_case(golden, case)
+    ctx = make_ctx(g["pos"].shape[0], g["params"], g["pos"], g["vel"], g["mass"])
+    for s, dt in enumerate(g["dts"]):
+        ctx.step(float(dt))
+        out = ctx.download(acc=False)
+        assert_bits(out["pos"], g["traj_pos"][s], f"pos@{s}")
+        assert_bits(out["vel"], g["traj_vel"][s], f"vel@{s}")
+        assert_bits(out["rho"], g["traj_rho"][s], f"rho@{s}")
+        assert_bits(out["pressure"], g["traj_pressure"][s], f"P@{s}")
+        t, _ = ctx.time()
+        assert np.float32(t) == g["traj_time"][s]
+
+
+# ---- against the oracle on the dam-break workloads ------------------------------------
+
+def test_gpu_10k_dam_break_trajectory_fixed_and_adaptive(port):
+    w = I.config0()
+    for dt in (1e-3, 0.0):
+        ctx = make_ctx(w.n, w.params, w.pos, w.vel, w.mass)
+        e = O.Engine(port, w.n)
+        e.initialize(w.params)
+        e.add(w.pos, w.vel, w.mass)
+        for s in range(12):
+            ctx.step(dt)
+            e.step(dt)
+            out = ctx.download()
+            ref = e.get()
+            for k in ("pos", "vel", "rho", "pressure", "acc"):
+                assert_bits(out[k], ref[k], f"{k}@{s} dt={dt}")
+            t, last = ctx.time()
+            assert t == e.time() and last == e.last_dt()
+        st = ctx.stats()
+        d = e.diag()
+        assert st["max_neighbors"] == d[4]
+        assert st["total_neighbor_queries"] == d[5]
+
+
+def test_gpu_neighbour_lists_100k(port):
+    w = I.scaled_dam_break(100_000, seed=5)
+    ctx = make_ctx(w.n, w.params, w.pos, w.vel, w.mass)
+    c_gpu, i_gpu = ctx.pairs()
+    c_ref, i_ref = port.query(w.pos, 0.04)
+    assert np.array_equal(c_gpu, c_ref)
+    assert np.array_equal(i_gpu, i_ref)
+
+
+def test_gpu_1M_dam_break_fresh_step_bit_exact(port):
+    """Configuration 1 (1,000,000 particles): one field evaluation and one step from the
+    initial state, every field bit-identical to the oracle."""
+    w = I.config1()
+    ctx = make_ctx(w.n, w.params, w.pos, w.vel, w.mass)
+    ctx.eval()
+    out = ctx.download()
+    rho, P, acc = port.fields(w.pos, w.vel, w.mass, w.params)
+    assert_bits(out["rho"], rho, "rho")
+    assert_bits(out["pressure"], P, "P")
+    assert_bits(out["acc"], acc, "acc")
+    e = O.Engine(port, w.n)
+    e.initialize(w.params)
+    e.add(w.pos, w.vel, w.mass)
+    e.step(w.dt)
+    ctx.step(w.dt)
+    out = ctx.download(acc=False)
+    ref = e.get()
+    for k in ("pos", "vel", "rho", "pressure"):
+        assert_bits(out[k], ref[k], k)
+
+
+def test_gpu_density_error_against_fp64(port):
+    """Stated accuracy: density relative error <= 1e-5 against the FP64 re-evaluation."""
+    w = I.scaled_dam_break(200_000, seed=3)
+    ctx = make_ctx(w.n, w.params, w.pos, w.vel, w.mass)
+    ctx.eval()
+    rho = ctx.download()["rho"].astype(np.float64)
+    rho64, _, _ = port.fields_f64(w.pos, w.vel, w.mass, w.params)
+    rel = np.abs(rho - rho64) / np.abs(rho64)
+    assert rel.max() <= 1e-5, rel.max()
+
+
+def test_gpu_fresh_state_restore(port):
+    w = I.config0()
+    ctx = make_ctx(w.n, w.params, w.pos, w.vel, w.mass)
+    ctx.snapshot()
+    ctx.step(w.dt)
+    a = ctx.download()
+    for _ in range(3):
+        ctx.restore()
+        ctx.step(w.dt)
+        b = ctx.download()
+        for k in ("pos", "vel", "rho"):
+            assert_bits(a[k], b[k], k)
+
+
+# ---- edge cases ----------------------------------------------------------------------
+
+def test_gpu_single_particle_and_empty(port):
+    prm = I.params16()
+    ctx = sphx.Context(8)
+    ctx.set_params(prm)
+    ctx.step(1e-3)  # empty: no-op
+    assert ctx.time()[0] == 0.0
+    pos = np.array([[0.1, 0.2, 0.3]], np.float32)
+    ctx.upload(pos, None, np.array([1e-3], np.float32))
+    ctx.step(1e-3)
+    e = O.Engine(port, 8)
+    e.initialize(prm)
+    e.add(pos, None, np.array([1e-3], np.float32))
+    e.step(1e-3)
+    out, ref = ctx.download(), e.get()
+    for k in ("pos", "vel", "rho", "pressure"):
+        assert_bits(out[k], ref[k], k)
+
+
+def test_gpu_all_particles_in_one_cell_and_coincident(port):
+    rng = np.random.default_rng(4)
+    pos = (0.5 + rng.random((700, 3)) * 0.03).astype(np.float32)
+    pos[100:140] = pos[99]  # 41 coincident particles
+    vel = (rng.standard_normal((700, 3)) * 0.1).astype(np.float32)
+    mass = np.full(700, 1e-3, np.float32)
+    prm = I.params16(xmin=0, xmax=1, ymin=0, ymax=1, zmin=0, zmax=1)
+    ctx = make_ctx(700, prm, pos, vel, mass)
+    c1, i1 = ctx.pairs()
+    c2, i2 = port.query(pos, 0.04)
+    assert np.array_equal(c1, c2) and np.array_equal(i1, i2)
+    ctx.eval()
+    out = ctx.download()
+    for a, b, k in zip((out["rho"], out["pressure"], out["acc"]),
+                       port.fields(pos, vel, mass, prm), ("rho", "P", "acc")):
+        assert_bits(a, b, k)
+
+
+def test_gpu_capacity_and_parameter_errors():
+    ctx = sphx.Context(4)
+    with pytest.raises(sphx.SphxError) as ei:
+        ctx.upload(np.zeros((5, 3), np.float32), None, np.ones(5, np.float32))
+    assert ei.value.code == -5
+    with pytest.raises(sphx.SphxError) as ei:
+        ctx.set_params(I.params16(neighbor_search_radius=0.0))
+    assert ei.value.code == -1
+    ctx.upload(np.zeros((2, 3), np.float32), None, np.ones(2, np.float32))
+    with pytest.raises(sphx.SphxError) as ei:
+        ctx.step(1e-3)  # no parameters yet
+    assert ei.value.code == -6
+
+
+def test_gpu_domain_too_large_is_an_error_not_a_fault():
+    ctx = sphx.Context(4, max_grid_cells=1000)
+    ctx.set_params(I.params16())
+    pos = np.array([[0, 0, 0], [10, 10, 10]], np.float32)
+    ctx.upload(pos, None, np.ones(2, np.float32))
+    ctx.step(1e-3)
+    with pytest.raises(sphx.SphxError) as ei:
+        ctx.download()
+    assert ei.value.code == -7
