@@ -39,7 +39,7 @@ extern "C" {
 #define SPHX_ERR_TIMEOUT (-4)      /* a bounded device-side wait gave up */
 #define SPHX_ERR_CAPACITY (-5)     /* more particles than the context's capacity */
 #define SPHX_ERR_NOT_READY (-6)    /* no parameters or no particles yet */
-#define SPHX_ERR_DOMAIN (-7)       /* occupied cell box too large for the cell grid */
+#define SPHX_ERR_DOMAIN (-7)       /* cell grid cannot be laid out (reserved) */
 #define SPHX_ERR_OVERFLOW (-8)     /* caller's output buffer too small */
 
 /* SPHParameters (src/sph_engine.h:14-34), same fields, same order, same meaning. */
@@ -64,7 +64,8 @@ typedef struct sphx_tuning {
     int mode;              /* SPHX_MODE_* (default EXACT) */
     int warps_per_block;   /* neighbour-pass CTA size in warps; 0 = default (4) */
     int blocks_per_sm;     /* persistent CTAs per SM for the neighbour passes; 0 = auto */
-    int64_t max_grid_cells;/* cap on the dense cell grid (cells); 0 = default */
+    int64_t max_grid_cells;/* cap on the dense cell grid (cells), >= 125; a larger box of
+                              occupied cells is folded per axis; 0 = default */
     int profile;           /* 1 = time each phase with CUDA events (read back lazily) */
 } sphx_tuning;
 

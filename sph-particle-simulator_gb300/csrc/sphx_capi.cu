@@ -205,7 +205,7 @@ const char* sphx_strerror(int code) {
         case SPHX_ERR_TIMEOUT: return "device-side wait timed out";
         case SPHX_ERR_CAPACITY: return "particle capacity exceeded";
         case SPHX_ERR_NOT_READY: return "parameters or particles not set";
-        case SPHX_ERR_DOMAIN: return "occupied cell box exceeds the cell grid capacity";
+        case SPHX_ERR_DOMAIN: return "cell grid cannot be laid out";
         case SPHX_ERR_OVERFLOW: return "output buffer too small";
         default: return "unknown sphx error";
     }
@@ -245,6 +245,7 @@ int sphx_create(sphx_ctx** out, size_t capacity, const sphx_tuning* tuning) {
         if (max_cells < (int64_t)1 << 24) max_cells = (int64_t)1 << 24;
     }
     if (max_cells > ((int64_t)1 << 31) - 4) max_cells = ((int64_t)1 << 31) - 4;
+    if (max_cells < 125) max_cells = 125;  // a folded axis needs >= 5 cells
     c->sc.max_cells = (uint32_t)max_cells;
     Buffers& b = c->b;
     const size_t C = capacity;

@@ -4,9 +4,10 @@
 //
 // Cells are the reference's own: floor(x * inv_cell) per axis with
 // inv_cell = 1.0f / neighbor_search_radius (spatial_hash.h:30-36, 63-66).  Instead of a
-// hash map of index vectors the occupied-cell box is laid out as a dense grid with a
-// linear key ((cx * dy + cy) * dz + cz), the keys are radix-sorted stably from insertion
-// order, and off[c] holds the first sorted position of cell c.  z is the fastest axis, so
+// hash map of index vectors the occupied-cell box is laid out as a dense grid (folded
+// per axis when the box is huge, see k_grid_setup) with a linear key
+// ((cx * dy + cy) * dz + cz), the keys are radix-sorted stably from insertion order, and
+// off[c] holds the first sorted position of cell c.  z is the fastest axis, so
 // the three cells (cx+dx, cy+dy, cz-1..cz+1) of one stencil row are one contiguous range
 // of the sorted arrays.  Particles with a NaN/inf coordinate get key == ncells: they sort
 // last and are never anyone's neighbour (every distance test with them fails in the
@@ -126,6 +127,12 @@ __global__ void k_bbox(const float4* __restrict__ pos4, int n, float inv_cell, D
     }
 }
 
+// Grid extent.  The occupied-cell box is laid out densely when it has at most max_cells
+// cells.  Otherwise (particles spread over a huge box) every axis longer than F =
+// floor(cbrt(max_cells)) >= 256 cells is folded: its cell index is taken modulo F.  Cells
+// that fold onto each other are at least F - 2 cells apart, so a candidate from a folded
+// neighbour fails the distance test; sets and visiting order are unchanged, only the
+// number of candidates grows.
 __global__ void k_grid_setup(int n, uint32_t max_cells, DevState* ds) {
     if (threadIdx.x != 0) return;
     if ((int)ds->nonfinite >= n) {  // no finite particle: a one-cell grid, all keys sentinel
@@ -134,19 +141,24 @@ __global__ void k_grid_setup(int n, uint32_t max_cells, DevState* ds) {
             ds->cmax[a] = 0;
         }
     }
+    long long d[3];
     unsigned long long cells = 1;
+    bool fits = true;
     for (int a = 0; a < 3; ++a) {
-        const long long d = (long long)ds->cmax[a] - (long long)ds->cmin[a] + 1;
-        ds->dim[a] = (int)(d < 0x7fffffff ? d : 0x7fffffff);
-        cells = (d > (long long)max_cells) ? (unsigned long long)max_cells + 1
-                                           : cells * (unsigned long long)d;
-        if (cells > (unsigned long long)max_cells) cells = (unsigned long long)max_cells + 1;
+        d[a] = (long long)ds->cmax[a] - (long long)ds->cmin[a] + 1;
+        if (d[a] > (long long)max_cells) fits = false;
+        else if ((cells *= (unsigned long long)d[a]) > (unsigned long long)max_cells) fits = false;
     }
-    if (cells > (unsigned long long)max_cells) {
-        ds->status = SPHX_ERR_DOMAIN;
-        ds->ncells = 0;
-        ds->passes = 0;
-        return;
+    long long fold = 1;
+    if (!fits) {
+        while ((fold + 1) * (fold + 1) * (fold + 1) <= (long long)max_cells) ++fold;
+    }
+    cells = 1;
+    for (int a = 0; a < 3; ++a) {
+        const bool w = !fits && d[a] > fold;
+        ds->wrap[a] = w ? 1 : 0;
+        ds->dim[a] = (int)(w ? fold : d[a]);
+        cells *= (unsigned long long)ds->dim[a];
     }
     ds->ncells = (uint32_t)cells;
     const int bits = 32 - __clz(ds->ncells);  // key range is [0, ncells]
@@ -157,14 +169,15 @@ __global__ void k_keys(const float4* __restrict__ pos4, int n, float inv_cell,
                        const DevState* ds, uint32_t* __restrict__ keys) {
     if (ds->status) return;
     const int cx0 = ds->cmin[0], cy0 = ds->cmin[1], cz0 = ds->cmin[2];
-    const uint32_t dy = ds->dim[1], dz = ds->dim[2], nc = ds->ncells;
+    const uint32_t dx = ds->dim[0], dy = ds->dim[1], dz = ds->dim[2], nc = ds->ncells;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 p = pos4[i];
         uint32_t key = nc;
         if (finite3(p.x, p.y, p.z)) {
-            const uint32_t x = (uint32_t)(cell_coord(p.x, inv_cell) - cx0);
-            const uint32_t y = (uint32_t)(cell_coord(p.y, inv_cell) - cy0);
-            const uint32_t z = (uint32_t)(cell_coord(p.z, inv_cell) - cz0);
+            // relative cell index (< 2^31), folded on the axes that wrap
+            const uint32_t x = (uint32_t)(cell_coord(p.x, inv_cell) - cx0) % dx;
+            const uint32_t y = (uint32_t)(cell_coord(p.y, inv_cell) - cy0) % dy;
+            const uint32_t z = (uint32_t)(cell_coord(p.z, inv_cell) - cz0) % dz;
             key = (x * dy + y) * dz + z;
         }
         keys[i] = key;

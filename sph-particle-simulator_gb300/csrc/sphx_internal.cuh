@@ -41,7 +41,8 @@ struct StepConst {
 struct DevState {
     int status;                 // 0 or SPHX_ERR_* raised on the device
     int cmin[3], cmax[3];       // box of occupied cells (finite particles)
-    int dim[3];                 // grid extent in cells
+    int dim[3];                 // grid extent in cells per axis
+    int wrap[3];                // 1: the axis is folded (cell index taken modulo dim)
     uint32_t ncells;            // dim product; also the key of non-finite particles
     uint32_t passes;            // radix passes needed this step
     uint32_t n_tiles;           // warp work items
@@ -49,7 +50,6 @@ struct DevState {
     uint32_t vmax_bits;         // max |v| (float bits) for the CFL rule
     uint32_t occupied;          // occupied cells
     uint32_t max_occ;           // particles in the fullest cell
-    uint32_t pad0;
     float dt;                   // dt of the current step
     float time;                 // current_time_
     float a0[4];                // accelerations_[0] (persists across steps)

@@ -63,23 +63,53 @@ __device__ __forceinline__ void tile_setup(const StepConst& c, const Buffers& b,
     }
 }
 
-// Calls f(begin, end) for every stencil row of the tile, in the reference's order.
+// Calls f(begin, end) for every stencil row of the tile, in the reference's order.  On a
+// folded axis the neighbour index wraps; a row that wraps on z is two segments, visited
+// in dz order.
 template <class F>
 __device__ __forceinline__ void for_each_row(const Buffers& b, const DevState* ds,
                                              const Tile& T, F&& f) {
     if (!T.cells) return;
     const int d0 = ds->dim[0], d1 = ds->dim[1], d2 = ds->dim[2];
-    const int z0 = max(T.cz + T.lo[2], 0), z1 = min(T.cz + T.hi[2], d2 - 1);
-    if (z0 > z1) return;
+    const bool w0 = ds->wrap[0], w1 = ds->wrap[1], w2 = ds->wrap[2];
+    // z range of every row: [z0, z1] plus, when z wraps past the end, [0, z2]
+    int z0 = T.cz + T.lo[2], z1 = T.cz + T.hi[2], z2 = -1;
+    int zp = -1, zq = -2;  // a wrapped piece at the front (dz < 0 past 0)
+    if (w2) {
+        if (z0 < 0) {
+            zp = z0 + d2;
+            zq = d2 - 1;
+            z0 = 0;
+        }
+        if (z1 >= d2) {
+            z2 = z1 - d2;
+            z1 = d2 - 1;
+        }
+    } else {
+        z0 = max(z0, 0);
+        z1 = min(z1, d2 - 1);
+    }
     for (int dx = T.lo[0]; dx <= T.hi[0]; ++dx) {
-        const int X = T.cx + dx;
-        if (X < 0 || X >= d0) continue;
+        int X = T.cx + dx;
+        if (w0) X = (X + d0) % d0;
+        else if (X < 0 || X >= d0) continue;
         for (int dy = T.lo[1]; dy <= T.hi[1]; ++dy) {
-            const int Y = T.cy + dy;
-            if (Y < 0 || Y >= d1) continue;
+            int Y = T.cy + dy;
+            if (w1) Y = (Y + d1) % d1;
+            else if (Y < 0 || Y >= d1) continue;
             const uint32_t rb = ((uint32_t)X * (uint32_t)d1 + (uint32_t)Y) * (uint32_t)d2;
-            const uint32_t a = b.off[rb + z0], e = b.off[rb + z1 + 1];
-            if (a < e) f((int)a, (int)e);
+            if (zp <= zq) {
+                const uint32_t a = b.off[rb + zp], e = b.off[rb + zq + 1];
+                if (a < e) f((int)a, (int)e);
+            }
+            if (z0 <= z1) {
+                const uint32_t a = b.off[rb + z0], e = b.off[rb + z1 + 1];
+                if (a < e) f((int)a, (int)e);
+            }
+            if (z2 >= 0) {
+                const uint32_t a = b.off[rb], e = b.off[rb + z2 + 1];
+                if (a < e) f((int)a, (int)e);
+            }
         }
     }
 }

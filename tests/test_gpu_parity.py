@@ -198,12 +198,27 @@ def test_gpu_capacity_and_parameter_errors():
     assert ei.value.code == -6
 
 
-def test_gpu_domain_too_large_is_an_error_not_a_fault():
-    ctx = sphx.Context(4, max_grid_cells=1000)
-    ctx.set_params(I.params16())
-    pos = np.array([[0, 0, 0], [10, 10, 10]], np.float32)
-    ctx.upload(pos, None, np.ones(2, np.float32))
-    ctx.step(1e-3)
-    with pytest.raises(sphx.SphxError) as ei:
-        ctx.download()
-    assert ei.value.code == -7
+@pytest.mark.parametrize("max_cells", [125, 1000, 0])
+def test_gpu_huge_box_folds_the_grid(port, max_cells):
+    """Particles spread over a box far larger than the cell grid: the grid folds, and
+    lists, order and fields stay bit-identical (cells that fold together are far apart)."""
+    rng = np.random.default_rng(8)
+    clusters = [np.array(c, np.float32) for c in ((0, 0, 0), (10, 10, 10), (3.3, -7.1, 0.2),
+                                                   (250.0, 0.0, -40.0))]
+    pos = np.concatenate([c + rng.random((300, 3)).astype(np.float32) * 0.12 for c in clusters])
+    n = pos.shape[0]
+    vel = (rng.standard_normal((n, 3)) * 0.1).astype(np.float32)
+    mass = np.full(n, 1e-3, np.float32)
+    prm = I.params16(xmin=-100, xmax=300, ymin=-100, ymax=100, zmin=-100, zmax=100)
+    ctx = make_ctx(n, prm, pos, vel, mass, max_grid_cells=max_cells)
+    c1, i1 = ctx.pairs()
+    c2, i2 = port.query(pos, 0.04)
+    assert np.array_equal(c1, c2) and np.array_equal(i1, i2)
+    ctx.eval()
+    out = ctx.download()
+    for a, b, k in zip((out["rho"], out["pressure"], out["acc"]),
+                       port.fields(pos, vel, mass, prm), ("rho", "P", "acc")):
+        assert_bits(a, b, k)
+    st = ctx.stats()
+    if max_cells:
+        assert st["grid_cells"] <= max(max_cells, 125)
