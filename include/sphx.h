@@ -170,6 +170,33 @@ int sphx_restore(sphx_ctx* ctx);
  * (sphx_download returns zeros for them until the next step or eval). */
 int sphx_debug_pairs(sphx_ctx* ctx, int64_t* counts, int64_t* idx, size_t* total_inout);
 
+/* ---- density evaluation that allocates nothing ----------------------------------------
+ * No counterpart in the reference (its step always allocates: SPHEngine resizes its
+ * buffers and builds fresh neighbour vectors every step).  For callers that must not
+ * allocate device memory -- an application that owns the whole device-memory budget and
+ * hands libraries pointers into it, or a per-frame loop that cannot afford the device
+ * synchronisation a cudaMalloc/cudaFree brings.
+ *
+ * Computes rho and P (compute_densities / compute_pressures, src/sph_engine.cpp:203-224)
+ * of n particles, bit-identical to sphx_eval + sphx_download.  pos_xyz (3n floats), mass
+ * (n), rho (n) and pressure (n) are DEVICE pointers owned by the caller, in insertion
+ * order; rho or pressure may be NULL.  Enqueued on cuda_stream (NULL: the default
+ * stream) and asynchronous: results are ready when that stream reaches the call.
+ * Working memory is one fixed file-scope device array inside the library (about 8 MiB,
+ * held by every GPU that loads the library until exit); the function itself calls no
+ * allocator.  Rules:
+ *  - n > SPHX_NOALLOC_MAX_PARTICLES -> SPHX_ERR_CAPACITY, nothing launched;
+ *  - occupied-cell boxes larger than SPHX_NOALLOC_MAX_CELLS cells are folded (results
+ *    unchanged);
+ *  - every call shares the one array: calls that overlap on the GPU (several streams or
+ *    host threads at once) race and must be serialised by the caller;
+ *  - the first call on a device looks up the array's device address with that device
+ *    current; make that first call before any stream capture begins. */
+#define SPHX_NOALLOC_MAX_PARTICLES 65536
+#define SPHX_NOALLOC_MAX_CELLS 262144
+int sphx_density_noalloc(const sphx_params* params, size_t n, const float* pos_xyz,
+                         const float* mass, float* rho, float* pressure, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,189 @@
+// sphx_density_noalloc: the density + pressure evaluation for callers that must not
+// allocate device memory.
+//
+// Some host applications own every byte of device memory: an engine or visualiser that
+// embeds the SPH step reserves a fixed budget up front and hands libraries pointers into
+// it, and in a per-frame loop a cudaMalloc/cudaFree would also synchronise the device and
+// stall the frame.  Those callers cannot use the context API (sphx_create allocates the
+// step's buffers).  This entry point takes device pointers for its inputs and outputs and
+// keeps all of its working memory -- packed and cell-sorted particle copies, radix-sort
+// keys and permutation, the cell grid, the tile list, the device-side step state -- in
+// one file-scope __device__ array of fixed size (kNoAllocScratchBytes, about 8 MiB),
+// which every GPU that loads the library holds until the process exits.  It runs the same
+// kernels as sphx_eval's grid build and density pass, so its results are those of
+// sphx_eval + sphx_download.
+//
+// Limits and rules (also in include/sphx.h):
+//  - at most SPHX_NOALLOC_MAX_PARTICLES particles per call; larger n is rejected with
+//    SPHX_ERR_CAPACITY before anything is launched;
+//  - the cell grid has SPHX_NOALLOC_MAX_CELLS cells; a larger box of occupied cells is
+//    folded onto it (results unchanged, more candidates to test);
+//  - all calls share the one array, which keeps the previous call's contents: the
+//    device-side step state is cleared at the start of every call, every other region is
+//    fully written before it is read.  Calls whose work overlaps on the GPU (two streams,
+//    two host threads) race on the array and must be serialised by the caller;
+//  - the first call on a device looks up the array's device address
+//    (cudaGetSymbolAddress) with that device current; make that first call before any
+//    stream capture begins.
+#include <cmath>
+#include <mutex>
+
+#include "sphx_internal.cuh"
+
+using namespace sphx;
+
+namespace {
+
+constexpr size_t kAlign = 256;
+constexpr size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+constexpr size_t kN = SPHX_NOALLOC_MAX_PARTICLES;
+constexpr size_t kCells = SPHX_NOALLOC_MAX_CELLS;
+constexpr size_t kRadixBlocks = (kN + kRadixTileN - 1) / kRadixTileN;
+constexpr size_t kHist = kRadixBlocks * kRadixBuckets;
+constexpr size_t kScanPart =
+    ((kHist + kScanTileN - 1) / kScanTileN > (kN + kScanTileN - 1) / kScanTileN
+         ? (kHist + kScanTileN - 1) / kScanTileN
+         : (kN + kScanTileN - 1) / kScanTileN) + 1;
+
+// byte offsets of the regions inside the scratch array
+constexpr size_t kOffState = 0;
+constexpr size_t kOffPos4 = kOffState + align_up(sizeof(DevState));
+constexpr size_t kOffVel4 = kOffPos4 + align_up(kN * sizeof(float4));
+constexpr size_t kOffPos4s = kOffVel4 + align_up(kN * sizeof(float4));
+constexpr size_t kOffVel4s = kOffPos4s + align_up(kN * sizeof(float4));
+constexpr size_t kOffAux4s = kOffVel4s + align_up(kN * sizeof(float4));
+constexpr size_t kOffKey0 = kOffAux4s + align_up(kN * sizeof(float4));
+constexpr size_t kOffKey1 = kOffKey0 + align_up(kN * sizeof(uint32_t));
+constexpr size_t kOffVal0 = kOffKey1 + align_up(kN * sizeof(uint32_t));
+constexpr size_t kOffVal1 = kOffVal0 + align_up(kN * sizeof(uint32_t));
+constexpr size_t kOffKeyS = kOffVal1 + align_up(kN * sizeof(uint32_t));
+constexpr size_t kOffIdS = kOffKeyS + align_up(kN * sizeof(uint32_t));
+constexpr size_t kOffTiles = kOffIdS + align_up(kN * sizeof(uint32_t));
+constexpr size_t kOffOff = kOffTiles + align_up(kN * sizeof(uint32_t));
+constexpr size_t kOffHist = kOffOff + align_up((kCells + 2) * sizeof(uint32_t));
+constexpr size_t kOffScan = kOffHist + align_up(kHist * sizeof(uint32_t));
+constexpr size_t kNoAllocScratchBytes = kOffScan + align_up(kScanPart * sizeof(uint32_t));
+
+// The scratch.  In host code this name is only a host-side stand-in for the device
+// array: its device address comes from cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mutex;
+unsigned char* g_scratch_addr[kMaxDevices] = {};
+int g_num_sms[kMaxDevices] = {};
+
+// Looks up (once per device, with that device current) the device address of the
+// scratch array and the SM count.
+int setup_device(int dev, unsigned char** addr, int* sms) {
+    if (dev < 0 || dev >= kMaxDevices) return SPHX_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    if (!g_scratch_addr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p)
+            return SPHX_ERR_CUDA;
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return SPHX_ERR_CUDA;
+        g_num_sms[dev] = n > 0 ? n : 1;
+        g_scratch_addr[dev] = static_cast<unsigned char*>(p);
+    }
+    *addr = g_scratch_addr[dev];
+    *sms = g_num_sms[dev];
+    return SPHX_OK;
+}
+
+// W_3d (kernels.cpp:58-66) on the host, for the self term W(0); built with
+// -ffp-contract=off like the rest of the library's host code.
+float noalloc_cubic_w(float sigma, float q) {
+    if (q >= 0.0f && q <= 1.0f) return sigma * (2.0f / 3.0f - q * q + 0.5f * q * q * q);
+    if (q > 1.0f && q <= 2.0f) {
+        const float tmp = 2.0f - q;
+        return sigma * (1.0f / 6.0f * tmp * tmp * tmp);
+    }
+    return 0.0f;
+}
+
+}  // namespace
+
+extern "C" int sphx_density_noalloc(const sphx_params* p, size_t n, const float* pos_xyz,
+                                    const float* mass, float* rho, float* pressure,
+                                    void* cuda_stream) {
+    if (!p) return SPHX_ERR_INVALID_ARG;
+    if (n > kN) return SPHX_ERR_CAPACITY;
+    if (n == 0) return SPHX_OK;
+    if (!pos_xyz || !mass || (!rho && !pressure)) return SPHX_ERR_INVALID_ARG;
+    const float r = p->neighbor_search_radius;
+    if (!(r > 0.0f) || !std::isfinite(r) || !std::isfinite(1.0f / r)) return SPHX_ERR_INVALID_ARG;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return SPHX_ERR_CUDA;
+    unsigned char* base = nullptr;
+    int sms = 0;
+    int rc = setup_device(dev, &base, &sms);
+    if (rc) return rc;
+
+    // the step constants, computed exactly as sphx_set_params / sphx_eval do
+    StepConst c{};
+    c.n = (int)n;
+    c.inv_cell = 1.0f / r;
+    c.r2 = r * r;
+    const float h = p->smoothing_length;
+    c.h = h;
+    c.h_sq = h * h;
+    c.sigma = 1.0f / (static_cast<float>(M_PI) * h * h * h);
+    c.w0 = noalloc_cubic_w(c.sigma, std::sqrt(0.0f) / h);
+    c.rest = p->rest_density;
+    c.gas = p->gas_constant;
+    c.visc = p->viscosity;
+    c.grav = p->gravity;
+    c.damping = p->damping;
+    c.cfl = p->cfl_factor;
+    c.timestep = p->timestep;
+    c.lo[0] = p->xmin;
+    c.hi[0] = p->xmax;
+    c.lo[1] = p->ymin;
+    c.hi[1] = p->ymax;
+    c.lo[2] = p->zmin;
+    c.hi[2] = p->zmax;
+    c.max_cells = (uint32_t)kCells;
+
+    Buffers b{};
+    b.pos4 = reinterpret_cast<float4*>(base + kOffPos4);
+    b.vel4 = reinterpret_cast<float4*>(base + kOffVel4);
+    b.pos4_s = reinterpret_cast<float4*>(base + kOffPos4s);
+    b.vel4_s = reinterpret_cast<float4*>(base + kOffVel4s);
+    b.aux4_s = reinterpret_cast<float4*>(base + kOffAux4s);
+    b.acc4_s = nullptr;  // not touched by the grid build or the density pass
+    b.key[0] = reinterpret_cast<uint32_t*>(base + kOffKey0);
+    b.key[1] = reinterpret_cast<uint32_t*>(base + kOffKey1);
+    b.val[0] = reinterpret_cast<uint32_t*>(base + kOffVal0);
+    b.val[1] = reinterpret_cast<uint32_t*>(base + kOffVal1);
+    b.key_s = reinterpret_cast<uint32_t*>(base + kOffKeyS);
+    b.id_s = reinterpret_cast<uint32_t*>(base + kOffIdS);
+    b.tile_start = reinterpret_cast<uint32_t*>(base + kOffTiles);
+    b.off = reinterpret_cast<uint32_t*>(base + kOffOff);
+    b.hist = reinterpret_cast<uint32_t*>(base + kOffHist);
+    b.scan_part = reinterpret_cast<uint32_t*>(base + kOffScan);
+    b.diag_part = nullptr;
+    b.radix_blocks = (int)kRadixBlocks;
+    b.scan_part_cap = (int)kScanPart;
+    b.diag_blocks = 0;
+    DevState* ds = reinterpret_cast<DevState*>(base + kOffState);
+
+    LaunchCtx L{};
+    L.stream = static_cast<cudaStream_t>(cuda_stream);
+    L.num_sms = sms;
+    L.warps_per_block = 4;
+    L.blocks_per_sm = 0;
+
+    // the previous call's device-side state must not leak into this one
+    if (cudaMemsetAsync(ds, 0, sizeof(DevState), L.stream) != cudaSuccess) return SPHX_ERR_CUDA;
+    launch_pack(L, (int)n, pos_xyz, nullptr, mass, b.pos4, b.vel4);
+    launch_begin_step(L, ds, 1);
+    launch_build_grid(L, c, b, ds);
+    launch_density(L, c, b, ds);
+    launch_unpack_sorted(L, (int)n, b.id_s, b.aux4_s, nullptr, rho, pressure, nullptr);
+    if (cudaGetLastError() != cudaSuccess) return SPHX_ERR_CUDA;
+    return SPHX_OK;
+}

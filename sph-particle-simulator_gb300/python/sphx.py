@@ -29,8 +29,9 @@ EXPORTS = (
     "sphx_version", "sphx_strerror", "sphx_create", "sphx_destroy", "sphx_set_stream",
     "sphx_set_params", "sphx_upload", "sphx_step", "sphx_eval", "sphx_download",
     "sphx_size", "sphx_get_time", "sphx_set_time", "sphx_get_stats", "sphx_reset_stats",
-    "sphx_snapshot", "sphx_restore", "sphx_debug_pairs",
+    "sphx_snapshot", "sphx_restore", "sphx_debug_pairs", "sphx_density_noalloc",
 )
+NOALLOC_MAX_PARTICLES = 65536
 
 
 class SphxParams(C.Structure):
@@ -98,6 +99,7 @@ def load_library(path: Path | str = LIB_PATH) -> C.CDLL:
         "sphx_snapshot": ([vp], C.c_int),
         "sphx_restore": ([vp], C.c_int),
         "sphx_debug_pairs": ([vp, fp, fp, C.POINTER(sz)], C.c_int),
+        "sphx_density_noalloc": ([C.POINTER(SphxParams), sz, fp, fp, fp, fp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -254,3 +256,15 @@ class Context:
         self._check(self._lib.sphx_debug_pairs(self._h, _ptr(counts), _ptr(idx),
                                                C.byref(total2)), "sphx_debug_pairs")
         return counts, idx[: total2.value]
+
+
+def density_noalloc(params16, n: int, pos_ptr: int, mass_ptr: int, rho_ptr: int | None,
+                    pressure_ptr: int | None, stream_ptr: int | None = None) -> None:
+    """sphx_density_noalloc on caller-owned DEVICE buffers (raw pointers); asynchronous on
+    the given stream."""
+    cv = lambda p: C.c_void_p(p) if p else None
+    rc = lib().sphx_density_noalloc(C.byref(params_struct(params16)), n, cv(pos_ptr),
+                                    cv(mass_ptr), cv(rho_ptr), cv(pressure_ptr),
+                                    cv(stream_ptr))
+    if rc != OK:
+        raise SphxError(rc, "sphx_density_noalloc")
