@@ -36,6 +36,8 @@ __global__ void k_begin_step(DevState* ds, int reset_bbox) {
     ds->occupied = 0;
     ds->max_occ = 0;
     ds->n_tiles = 0;
+    ds->work[0] = 0;
+    ds->work[1] = 0;
 }
 
 int launch_begin_step(const LaunchCtx& L, DevState* ds, int reset_bbox) {

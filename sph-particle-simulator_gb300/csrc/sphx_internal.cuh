@@ -50,6 +50,7 @@ struct DevState {
     uint32_t vmax_bits;         // max |v| (float bits) for the CFL rule
     uint32_t occupied;          // occupied cells
     uint32_t max_occ;           // particles in the fullest cell
+    uint32_t work[2];           // tile counters of the density and force passes
     float dt;                   // dt of the current step
     float time;                 // current_time_
     float a0[4];                // accelerations_[0] (persists across steps)

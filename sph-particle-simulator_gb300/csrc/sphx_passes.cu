@@ -128,43 +128,153 @@ __device__ __forceinline__ Diff diff(const float4& xi, const float4& xj) {
 }
 
 // ---------------------------------------------------------------------------------------
+// Chunk machinery shared by the density and force passes.
+//
+// A row segment is consumed in chunks of 32 candidates staged in shared memory.  For a
+// chunk, every lane first builds a 32-bit mask of its hits (the exact distance test; the
+// candidates a warp-uniform bounding-box test rules out for the whole tile are skipped).
+// The expensive per-pair terms are then computed FLATTENED: the warp's hits are listed
+// (lane, candidate) in lane-then-candidate order and the 32 lanes work through that list
+// together, writing each term to shared memory.  Finally every lane adds its own terms in
+// candidate order -- the reference's order -- so each particle's sums are the same
+// sequence of IEEE additions as in the reference, while the SIMT lanes stay busy on the
+// costly terms regardless of how unevenly the hits fall on lanes.
+// ---------------------------------------------------------------------------------------
+
+constexpr uint32_t kFull = 0xffffffffu;
+constexpr int kDensityBatch = 256;  // flattened terms computed per round (density)
+constexpr int kForceBatch = 128;    // flattened terms computed per round (force)
+
+__device__ __forceinline__ uint32_t warp_excl_scan(uint32_t v, int lane, uint32_t& total) {
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, x, o);
+        if (lane >= o) x += y;
+    }
+    total = __shfl_sync(kFull, x, 31);
+    return x - v;
+}
+
+// Axis-aligned box of the tile's particles (valid lanes).
+struct TileBox {
+    float lo[3], hi[3];
+};
+__device__ __forceinline__ TileBox tile_box(const float4& xi, bool valid) {
+    TileBox B;
+    const float inf = __int_as_float(0x7f800000);
+    B.lo[0] = valid ? xi.x : inf;
+    B.lo[1] = valid ? xi.y : inf;
+    B.lo[2] = valid ? xi.z : inf;
+    B.hi[0] = valid ? xi.x : -inf;
+    B.hi[1] = valid ? xi.y : -inf;
+    B.hi[2] = valid ? xi.z : -inf;
+#pragma unroll
+    for (int o = 16; o; o >>= 1)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            B.lo[a] = fminf(B.lo[a], __shfl_xor_sync(kFull, B.lo[a], o));
+            B.hi[a] = fmaxf(B.hi[a], __shfl_xor_sync(kFull, B.hi[a], o));
+        }
+    return B;
+}
+
+// Conservative: false only if no point of the box is within r of p (margin 1e-4 on r^2
+// covers every rounding of this test and of the exact distance test).
+__device__ __forceinline__ bool box_near(const TileBox& B, const float4& p, float r2_margin) {
+    const float ex = fmaxf(fmaxf(B.lo[0] - p.x, p.x - B.hi[0]), 0.0f);
+    const float ey = fmaxf(fmaxf(B.lo[1] - p.y, p.y - B.hi[1]), 0.0f);
+    const float ez = fmaxf(fmaxf(B.lo[2] - p.z, p.z - B.hi[2]), 0.0f);
+    return ex * ex + ey * ey + ez * ez <= r2_margin;
+}
+
+// Hit mask of this lane's particle against the staged chunk (candidates in `surv` only).
+__device__ __forceinline__ uint32_t chunk_hits(const float4* cand, uint32_t surv,
+                                               const float4& xi, float r2) {
+    uint32_t mask = 0;
+#pragma unroll
+    for (int jj = 0; jj < 32; ++jj) {
+        if (surv & (1u << jj)) {
+            const Diff d = diff(xi, cand[jj]);
+            if (d.d2 <= r2) mask |= 1u << jj;
+        }
+    }
+    return mask;
+}
+
+// Work distribution: warps take tiles from a per-pass counter (dynamic, so crowded cells
+// in degenerate states do not serialise the tail).
+__device__ __forceinline__ uint32_t next_tile(uint32_t* ctr, int lane) {
+    uint32_t t = 0;
+    if (lane == 0) t = atomicAdd(ctr, 1u);
+    return __shfl_sync(kFull, t, 0);
+}
+
+// ---------------------------------------------------------------------------------------
 // density + pressure:  rho_i = m_i W(0) + sum_{j in N(i), j != i} m_j W(r_ij)
 //                      P_i = k (rho_i - rho0)
 // (compute_density / compute_pressure, sph_engine.cpp:370-388)
 // ---------------------------------------------------------------------------------------
+struct DensitySmem {
+    float4 cand[32];
+    float4 tpos[32];
+    uint16_t plist[32 * 32];
+    float tbuf[kDensityBatch];
+};
+
 __global__ void __launch_bounds__(128) k_density(const StepConst c, const Buffers b,
                                                  DevState* ds) {
     if (ds->status) return;
-    extern __shared__ float4 smem_d[];
+    extern __shared__ __align__(16) unsigned char smem_raw_d[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float4* cand = smem_d + warp * kTile;
-    const int nwarps = gridDim.x * (blockDim.x >> 5);
+    DensitySmem* S = reinterpret_cast<DensitySmem*>(smem_raw_d) + warp;
     const uint32_t ntiles = ds->n_tiles;
+    const float r2m = c.r2 * 1.0001f;
+    const float inf = __int_as_float(0x7f800000);
     uint32_t my_max = 0;
-    for (uint32_t t = blockIdx.x * (blockDim.x >> 5) + warp; t < ntiles; t += nwarps) {
+    for (uint32_t t = next_tile(&ds->work[0], lane); t < ntiles; t = next_tile(&ds->work[0], lane)) {
         Tile T;
         float4 xi;
         bool valid;
         tile_setup(c, b, ds, t, lane, T, xi, valid);
         const int i = T.k0 + lane;
+        const TileBox B = tile_box(xi, valid);
+        S->tpos[lane] = xi;
         float rho = xmul(xi.w, c.w0);
         uint32_t nn = 0;
         for_each_row(b, ds, T, [&](int a, int e) {
             for (int s = a; s < e; s += kTile) {
                 const int m = min(kTile, e - s);
                 __syncwarp();
-                if (lane < m) cand[lane] = b.pos4_s[s + lane];
+                const float4 pl = lane < m ? b.pos4_s[s + lane] : make_float4(inf, inf, inf, 0.f);
+                S->cand[lane] = pl;
+                const uint32_t surv = __ballot_sync(kFull, box_near(B, pl, r2m));
                 __syncwarp();
-                for (int jj = 0; jj < m; ++jj) {
-                    const float4 xj = cand[jj];
-                    const Diff d = diff(xi, xj);
-                    if (valid && d.d2 <= c.r2) {
-                        ++nn;
-                        if (s + jj != i) {
-                            const float q = xdiv(xsqrt(d.d2), c.h);
-                            rho = xadd(rho, xmul(xj.w, cubic_w(c, q)));
-                        }
+                if (!surv) continue;
+                uint32_t mask = valid ? chunk_hits(S->cand, surv, xi, c.r2) : 0u;
+                nn += __popc(mask);
+                const int self = i - s;
+                if ((unsigned)self < 32u) mask &= ~(1u << self);
+                const uint32_t cnt = __popc(mask);
+                uint32_t H;
+                const uint32_t o = warp_excl_scan(cnt, lane, H);
+                if (!H) continue;
+                for (uint32_t mm = mask, k = o; mm; mm &= mm - 1, ++k)
+                    S->plist[k] = (uint16_t)((lane << 5) | (__ffs(mm) - 1));
+                __syncwarp();
+                for (uint32_t base = 0; base < H; base += kDensityBatch) {
+                    const uint32_t end = min(H, base + kDensityBatch);
+                    for (uint32_t f = base + lane; f < end; f += 32) {
+                        const uint32_t pr = S->plist[f];
+                        const float4 xj = S->cand[pr & 31];
+                        const Diff d = diff(S->tpos[pr >> 5], xj);
+                        const float q = xdiv(xsqrt(d.d2), c.h);
+                        S->tbuf[f - base] = xmul(xj.w, cubic_w(c, q));
                     }
+                    __syncwarp();
+                    const uint32_t k1 = min(o + cnt, end);
+                    for (uint32_t k = max(o, base); k < k1; ++k) rho = xadd(rho, S->tbuf[k - base]);
+                    __syncwarp();
                 }
             }
         });
@@ -173,9 +283,10 @@ __global__ void __launch_bounds__(128) k_density(const StepConst c, const Buffer
             b.aux4_s[i] = make_float4(rho, P, xmul(2.0f, rho), xdiv(xi.w, rho));
             my_max = max(my_max, nn);
         }
+        __syncwarp();
     }
 #pragma unroll
-    for (int o = 16; o; o >>= 1) my_max = max(my_max, __shfl_xor_sync(0xffffffffu, my_max, o));
+    for (int o = 16; o; o >>= 1) my_max = max(my_max, __shfl_xor_sync(kFull, my_max, o));
     if (lane == 0 && my_max) atomicMax(&ds->max_nn, (unsigned long long)my_max);
 }
 
@@ -185,19 +296,61 @@ __global__ void __launch_bounds__(128) k_density(const StepConst c, const Buffer
 //  sph_engine.cpp:390-443; integrate_leapfrog, cpp:290-310;
 //  ParticleSystem::apply_boundary_conditions, particle.cpp:122-153)
 // ---------------------------------------------------------------------------------------
+struct ForceSmem {
+    float4 cpos[32], cvel[32], caux[32];
+    float4 tpos[32], tvel[32];
+    float tP[32];
+    uint16_t plist[32 * 32];
+    float tb[6][kForceBatch];
+    unsigned char skip[kForceBatch];
+};
+
+// The pair term of particle t against candidate j: the pressure-force contribution
+// m_j * (P_t + P_j)/(2 rho_j) * gradW (subtracted by the caller; skipped when
+// |r| < 1e-6) and the viscosity contribution ((m_j/rho_j) mu (v_j - v_t)) laplacianW
+// (added), each with the reference's operations.
+__device__ __forceinline__ void force_term(const StepConst& c, const float4& xt,
+                                           const float4& vt, float Pt, const float4& xj,
+                                           const float4& vj, const float4& aj, float* p3,
+                                           float* v3, bool& skip) {
+    const Diff d = diff(xt, xj);
+    const float r_len = xsqrt(d.d2);
+    const float q = xdiv(r_len, c.h);
+    skip = r_len < 1e-6f;
+    p3[0] = p3[1] = p3[2] = 0.0f;
+    if (!skip) {
+        const float pt = xdiv(xadd(Pt, aj.y), aj.z);
+        float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+        if ((q >= 0.0f && q <= 1.0f) || (q > 1.0f && q <= 2.0f)) {
+            const float gf = cubic_grad_factor(c, q);
+            gx = xmul(gf, xdiv(d.x, r_len));
+            gy = xmul(gf, xdiv(d.y, r_len));
+            gz = xmul(gf, xdiv(d.z, r_len));
+        }
+        const float sp = xmul(xj.w, pt);
+        p3[0] = xmul(sp, xdiv(gx, c.h));
+        p3[1] = xmul(sp, xdiv(gy, c.h));
+        p3[2] = xmul(sp, xdiv(gz, c.h));
+    }
+    const float lap = cubic_lap(c, q);
+    const float sv = xmul(aj.w, c.visc);
+    v3[0] = xmul(xmul(sv, xsub(vj.x, vt.x)), lap);
+    v3[1] = xmul(xmul(sv, xsub(vj.y, vt.y)), lap);
+    v3[2] = xmul(xmul(sv, xsub(vj.z, vt.z)), lap);
+}
+
 template <bool kIntegrate>
-__global__ void __launch_bounds__(128) k_force(const StepConst c, const Buffers b,
+__global__ void __launch_bounds__(128, 6) k_force(const StepConst c, const Buffers b,
                                                DevState* ds) {
     if (ds->status) return;
-    extern __shared__ float4 smem_f[];
+    extern __shared__ __align__(16) unsigned char smem_raw_f[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float4* cp = smem_f + warp * (3 * kTile);
-    float4* cv = cp + kTile;
-    float4* ca = cv + kTile;
-    const int nwarps = gridDim.x * (blockDim.x >> 5);
+    ForceSmem* S = reinterpret_cast<ForceSmem*>(smem_raw_f) + warp;
     const uint32_t ntiles = ds->n_tiles;
     const float dt = ds->dt;
-    for (uint32_t t = blockIdx.x * (blockDim.x >> 5) + warp; t < ntiles; t += nwarps) {
+    const float r2m = c.r2 * 1.0001f;
+    const float inf = __int_as_float(0x7f800000);
+    for (uint32_t t = next_tile(&ds->work[1], lane); t < ntiles; t = next_tile(&ds->work[1], lane)) {
         Tile T;
         float4 xi;
         bool valid;
@@ -205,51 +358,72 @@ __global__ void __launch_bounds__(128) k_force(const StepConst c, const Buffers 
         const int i = T.k0 + lane;
         const float4 vi = valid ? b.vel4_s[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float Pi = valid ? b.aux4_s[i].y : 0.0f;
+        const TileBox B = tile_box(xi, valid);
+        S->tpos[lane] = xi;
+        S->tvel[lane] = vi;
+        S->tP[lane] = Pi;
         float fpx = 0.0f, fpy = 0.0f, fpz = 0.0f;
         float fvx = 0.0f, fvy = 0.0f, fvz = 0.0f;
         for_each_row(b, ds, T, [&](int a, int e) {
             for (int s = a; s < e; s += kTile) {
                 const int m = min(kTile, e - s);
                 __syncwarp();
-                if (lane < m) {
-                    cp[lane] = b.pos4_s[s + lane];
-                    cv[lane] = b.vel4_s[s + lane];
-                    ca[lane] = b.aux4_s[s + lane];
+                const bool in = lane < m;
+                const float4 pl = in ? b.pos4_s[s + lane] : make_float4(inf, inf, inf, 0.f);
+                S->cpos[lane] = pl;
+                const uint32_t surv = __ballot_sync(kFull, box_near(B, pl, r2m));
+                if (!surv) continue;
+                if (surv & (1u << lane)) {
+                    S->cvel[lane] = b.vel4_s[s + lane];
+                    S->caux[lane] = b.aux4_s[s + lane];
                 }
                 __syncwarp();
-                for (int jj = 0; jj < m; ++jj) {
-                    const float4 xj = cp[jj];
-                    const Diff d = diff(xi, xj);
-                    if (!(valid && d.d2 <= c.r2 && s + jj != i)) continue;
-                    const float4 aj = ca[jj];
-                    const float r_len = xsqrt(d.d2);
-                    const float q = xdiv(r_len, c.h);
-                    if (!(r_len < 1e-6f)) {
-                        const float pt = xdiv(xadd(Pi, aj.y), aj.z);
-                        float gx = 0.0f, gy = 0.0f, gz = 0.0f;
-                        if ((q >= 0.0f && q <= 1.0f) || (q > 1.0f && q <= 2.0f)) {
-                            const float gf = cubic_grad_factor(c, q);
-                            gx = xmul(gf, xdiv(d.x, r_len));
-                            gy = xmul(gf, xdiv(d.y, r_len));
-                            gz = xmul(gf, xdiv(d.z, r_len));
-                        }
-                        gx = xdiv(gx, c.h);
-                        gy = xdiv(gy, c.h);
-                        gz = xdiv(gz, c.h);
-                        const float sp = xmul(xj.w, pt);
-                        fpx = xsub(fpx, xmul(sp, gx));
-                        fpy = xsub(fpy, xmul(sp, gy));
-                        fpz = xsub(fpz, xmul(sp, gz));
+                uint32_t mask = valid ? chunk_hits(S->cpos, surv, xi, c.r2) : 0u;
+                const int self = i - s;
+                if ((unsigned)self < 32u) mask &= ~(1u << self);
+                const uint32_t cnt = __popc(mask);
+                uint32_t H;
+                const uint32_t o = warp_excl_scan(cnt, lane, H);
+                if (!H) continue;
+                for (uint32_t mm = mask, k = o; mm; mm &= mm - 1, ++k)
+                    S->plist[k] = (uint16_t)((lane << 5) | (__ffs(mm) - 1));
+                __syncwarp();
+                for (uint32_t base = 0; base < H; base += kForceBatch) {
+                    const uint32_t end = min(H, base + kForceBatch);
+                    for (uint32_t f = base + lane; f < end; f += 32) {
+                        const uint32_t pr = S->plist[f];
+                        const int tt = pr >> 5, jj = pr & 31;
+                        float p3[3], v3[3];
+                        bool sk;
+                        force_term(c, S->tpos[tt], S->tvel[tt], S->tP[tt], S->cpos[jj],
+                                   S->cvel[jj], S->caux[jj], p3, v3, sk);
+                        const uint32_t u = f - base;
+                        S->tb[0][u] = p3[0];
+                        S->tb[1][u] = p3[1];
+                        S->tb[2][u] = p3[2];
+                        S->tb[3][u] = v3[0];
+                        S->tb[4][u] = v3[1];
+                        S->tb[5][u] = v3[2];
+                        S->skip[u] = sk;
                     }
-                    const float4 vj = cv[jj];
-                    const float lap = cubic_lap(c, q);
-                    const float sv = xmul(aj.w, c.visc);
-                    fvx = xadd(fvx, xmul(xmul(sv, xsub(vj.x, vi.x)), lap));
-                    fvy = xadd(fvy, xmul(xmul(sv, xsub(vj.y, vi.y)), lap));
-                    fvz = xadd(fvz, xmul(xmul(sv, xsub(vj.z, vi.z)), lap));
+                    __syncwarp();
+                    const uint32_t k1 = min(o + cnt, end);
+                    for (uint32_t k = max(o, base); k < k1; ++k) {
+                        const uint32_t u = k - base;
+                        if (!S->skip[u]) {
+                            fpx = xsub(fpx, S->tb[0][u]);
+                            fpy = xsub(fpy, S->tb[1][u]);
+                            fpz = xsub(fpz, S->tb[2][u]);
+                        }
+                        fvx = xadd(fvx, S->tb[3][u]);
+                        fvy = xadd(fvy, S->tb[4][u]);
+                        fvz = xadd(fvz, S->tb[5][u]);
+                    }
+                    __syncwarp();
                 }
             }
         });
+        __syncwarp();
         if (!valid) continue;
         const float mi = xi.w;
         const float ax = xdiv(xadd(xadd(fpx, fvx), xmul(0.0f, mi)), mi);
@@ -326,6 +500,18 @@ __global__ void __launch_bounds__(128) k_pairs(const StepConst c, const Buffers 
     }
 }
 
+// Persistent grid: as many CTAs as fit on the GPU (queried once per kernel).
+template <class K>
+static int resident_blocks(const LaunchCtx& L, K kernel, int threads, size_t smem) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) !=
+            cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    if (L.blocks_per_sm > 0 && L.blocks_per_sm < per_sm) per_sm = L.blocks_per_sm;
+    return L.num_sms * per_sm;
+}
+
 static int pass_blocks(const LaunchCtx& L) {
     const int bps = L.blocks_per_sm > 0 ? L.blocks_per_sm : 8;
     return L.num_sms * bps;
@@ -333,19 +519,26 @@ static int pass_blocks(const LaunchCtx& L) {
 
 int launch_density(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds) {
     const int threads = 32 * L.warps_per_block;
-    const size_t sm = (size_t)L.warps_per_block * kTile * sizeof(float4);
-    k_density<<<pass_blocks(L), threads, sm, L.stream>>>(c, b, ds);
+    const size_t sm = (size_t)L.warps_per_block * sizeof(DensitySmem);
+    static int blocks[5] = {0, 0, 0, 0, 0};
+    if (!blocks[L.warps_per_block]) blocks[L.warps_per_block] = resident_blocks(L, k_density, threads, sm);
+    k_density<<<blocks[L.warps_per_block], threads, sm, L.stream>>>(c, b, ds);
     return 1;
 }
 
 int launch_force(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds,
                  int integrate) {
     const int threads = 32 * L.warps_per_block;
-    const size_t sm = (size_t)L.warps_per_block * 3 * kTile * sizeof(float4);
-    if (integrate)
-        k_force<true><<<pass_blocks(L), threads, sm, L.stream>>>(c, b, ds);
-    else
-        k_force<false><<<pass_blocks(L), threads, sm, L.stream>>>(c, b, ds);
+    const size_t sm = (size_t)L.warps_per_block * sizeof(ForceSmem);
+    static int blocks[2][5] = {{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}};
+    int& nb = blocks[integrate ? 1 : 0][L.warps_per_block];
+    if (integrate) {
+        if (!nb) nb = resident_blocks(L, k_force<true>, threads, sm);
+        k_force<true><<<nb, threads, sm, L.stream>>>(c, b, ds);
+    } else {
+        if (!nb) nb = resident_blocks(L, k_force<false>, threads, sm);
+        k_force<false><<<nb, threads, sm, L.stream>>>(c, b, ds);
+    }
     return 1;
 }
 
