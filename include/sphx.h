@@ -170,6 +170,27 @@ int sphx_restore(sphx_ctx* ctx);
  * (sphx_download returns zeros for them until the next step or eval). */
 int sphx_debug_pairs(sphx_ctx* ctx, int64_t* counts, int64_t* idx, size_t* total_inout);
 
+/* ---- standalone spatial hash (SpatialHash, src/spatial_hash.h:12-88) --------------------
+ * A cell grid of arbitrary positions on the GPU with the reference's query semantics:
+ * sphx_grid_query returns, for every query point p, the indices j with
+ * dot(p - x_j, p - x_j) <= radius_squared in the reference's order (stencil cells
+ * (dx,dy,dz) in [-cr,cr]^3 lexicographically, cr = ceil(sqrt(r2) * inv_cell) + 1, then
+ * insertion order), like SpatialHash::query_squared (src/spatial_hash.cpp:31-57). */
+typedef struct sphx_grid sphx_grid;
+int sphx_grid_create(sphx_grid** out, size_t capacity);
+void sphx_grid_destroy(sphx_grid* grid);
+/* SpatialHash::build (src/spatial_hash.cpp:15-25) with cells of cell_size; synchronises. */
+int sphx_grid_build(sphx_grid* grid, size_t n, const float* pos_xyz, float cell_size);
+/* Batched SpatialHash::query_squared: counts[nq]; idx (optional) receives the concatenated
+ * lists when *total_inout is large enough (else SPHX_ERR_OVERFLOW); *total_inout returns
+ * the number of entries. */
+int sphx_grid_query(sphx_grid* grid, size_t nq, const float* query_xyz, float radius_squared,
+                    int64_t* counts, int64_t* idx, size_t* total_inout);
+/* get_total_cells / get_max_particles_per_cell (src/spatial_hash.h:58-59). */
+int sphx_grid_info(sphx_grid* grid, size_t* occupied_cells, size_t* max_per_cell);
+/* get_cell_particles (src/spatial_hash.cpp:59-63): insertion indices of cell (x, y, z). */
+int sphx_grid_cell(sphx_grid* grid, int x, int y, int z, int64_t* idx, size_t* count_inout);
+
 /* ---- density evaluation that allocates nothing ----------------------------------------
  * No counterpart in the reference (its step always allocates: SPHEngine resizes its
  * buffers and builds fresh neighbour vectors every step).  For callers that must not

@@ -211,20 +211,20 @@ size_t ref_engine_get(void* e, float* pos, float* vel, float* rho, float* P) {
     return d.size();
 }
 
-// Per-particle record fields of get_particles() (src/particle.h:17-49), 17 floats each:
-// pos3 vel3 acc3 density pressure mass type temperature viscosity id color_r
+// Per-particle record fields of get_particles() (src/particle.h:17-49), 19 floats each:
+// pos3 vel3 acc3 density pressure mass type temperature viscosity id color3
 void ref_engine_particles(void* e, float* out) {
     const auto& ps = static_cast<sph::SPHEngine*>(e)->get_particles();
     for (size_t i = 0; i < ps.size(); ++i) {
         const sph::Particle& p = ps[i];
-        float* o = out + 17 * i;
+        float* o = out + 19 * i;
         o[0] = p.position.x; o[1] = p.position.y; o[2] = p.position.z;
         o[3] = p.velocity.x; o[4] = p.velocity.y; o[5] = p.velocity.z;
         o[6] = p.acceleration.x; o[7] = p.acceleration.y; o[8] = p.acceleration.z;
         o[9] = p.density; o[10] = p.pressure; o[11] = p.mass;
         o[12] = static_cast<float>(static_cast<int>(p.type));
         o[13] = p.temperature; o[14] = p.viscosity; o[15] = static_cast<float>(p.id);
-        o[16] = p.color.x;
+        o[16] = p.color.x; o[17] = p.color.y; o[18] = p.color.z;
     }
 }
 

@@ -1,0 +1,151 @@
+// GB300 drop-in for the reference's SPH engine (src/sph_engine.h).
+//
+// Same namespace, class names, members functions and semantics as the reference's
+// SPHParameters / SPHEngine / utils:: (src/sph_engine.h:14-204); SPHEngine::step runs on
+// the GPU through the sphx C ABI (include/sphx.h).  The particle set lives on the device;
+// the host ParticleSystem is a mirror kept in insertion order and synchronised lazily:
+// uploaded before a step when the host side changed (add_particles, clear_particles,
+// initialize_*), downloaded when read (get_particles, get_positions, ...).
+//
+// Differences from the reference, all deliberate:
+//  * PerformanceStats is public (the reference declares it private, which makes its own
+//    pybind11 module fail to compile, python/bindings.cpp:73).
+//  * Its timing fields are device times of the step's phases (CUDA events); the
+//    integration phase is fused into the force pass, so integration_time stays 0.
+//    max_neighbors / total_neighbor_queries are exact (the reference's are updated
+//    without synchronisation inside an OpenMP loop, sph_engine.cpp:350-351).
+//  * The kernel-function classes and equations:: free functions are not provided: the
+//    per-pair equations run only inside step(), on the GPU.
+//  * Device failures surface as std::runtime_error (the reference has none to report).
+#pragma once
+
+#include <cstddef>
+#include <memory>
+#include <vector>
+
+#include "particle.h"
+#include "spatial_hash.h"
+
+struct sphx_ctx;
+
+namespace sph {
+
+// Simulation parameters (src/sph_engine.h:14-34), same fields, defaults and order.
+struct SPHParameters {
+    float rest_density = 1000.0f;
+    float gas_constant = 2000.0f;
+    float viscosity = 0.001f;
+    float smoothing_length = 0.02f;
+    float particle_mass = 0.001f;
+    float timestep = 0.001f;
+    float gravity = -9.81f;
+    float damping = 0.99f;
+    float CFL_factor = 0.4f;
+
+    struct Boundaries {
+        float xmin = -1.0f, xmax = 1.0f;
+        float ymin = -1.0f, ymax = 1.0f;
+        float zmin = -1.0f, zmax = 1.0f;
+    } bounds;
+
+    float neighbor_search_radius = 0.04f;
+};
+
+class SPHEngine {
+   public:
+    // Per-phase timers and neighbour statistics (src/sph_engine.h:51-59), public here.
+    struct PerformanceStats {
+        double total_time = 0.0;
+        double neighbor_search_time = 0.0;
+        double density_computation_time = 0.0;
+        double force_computation_time = 0.0;
+        double integration_time = 0.0;
+        size_t max_neighbors = 0;
+        size_t total_neighbor_queries = 0;
+    };
+
+    explicit SPHEngine(size_t max_particles = 1000000);
+    ~SPHEngine();
+    SPHEngine(const SPHEngine&) = delete;
+    SPHEngine& operator=(const SPHEngine&) = delete;
+
+    void initialize(const SPHParameters& params);
+    void initialize_dam_break();
+    void initialize_fluid_drop();
+    void initialize_granular_flow();
+
+    void add_particles(const std::vector<Particle>& particles);
+    void clear_particles();
+
+    void step(float dt = 0.0f);  // dt <= 0: adaptive (CFL) timestep
+    void run_steps(size_t num_steps, bool adaptive_timestep = true);
+
+    const ParticleSystem& get_particles() const;
+    const SPHParameters& get_parameters() const { return params_; }
+    float get_current_time() const;
+    size_t get_step_count() const { return step_count_; }
+
+    void set_parameters(const SPHParameters& params);
+    void set_gravity(float gravity);
+    void set_viscosity(float viscosity);
+    void set_smoothing_length(float h);
+    void set_boundaries(float xmin, float xmax, float ymin, float ymax, float zmin, float zmax);
+
+    const PerformanceStats& get_performance_stats() const;
+    void reset_performance_stats();
+
+    void compute_conservation_errors(float& mass_error, float& energy_error) const;
+    float get_total_mass() const;
+    float get_total_energy() const;
+
+    std::vector<glm::vec3> get_positions() const;
+    std::vector<glm::vec3> get_velocities() const;
+    std::vector<float> get_densities() const;   // capacity-length, like the reference
+    std::vector<float> get_pressures() const;   // capacity-length, like the reference
+
+    void validate_simulation() const;
+    bool is_initialized() const { return initialized_; }
+
+    // GPU-side FP64 conservation sums of the state after the last step: mass, momentum
+    // (3), kinetic energy, potential energy (-m g y), sum of densities.
+    std::vector<double> get_conservation_sums() const;
+
+   private:
+    void push_params();
+    void sync_to_host() const;   // device -> host mirror, when the device is newer
+    void sync_to_device();       // host mirror -> device, when the host changed
+    void host_will_change();     // call before mutating the host mirror
+
+    mutable ParticleSystem particles_;
+    SPHParameters params_;
+    sphx_ctx* gpu_ = nullptr;
+    size_t step_count_ = 0;
+    bool initialized_ = false;
+    mutable bool host_stale_ = false;  // the device holds a newer state than the mirror
+    bool device_dirty_ = true;         // the mirror changed since the last upload
+    mutable std::vector<float> densities_;
+    mutable std::vector<float> pressures_;
+    mutable PerformanceStats perf_stats_;
+};
+
+// Integration methods (src/sph_engine.h:144-148); the step always uses leapfrog.
+enum class IntegrationMethod { EULER, VERLET, LEAPFROG };
+
+namespace utils {
+
+// Scene generators (src/sph_engine.cpp:450-552).
+std::vector<Particle> create_dam_break_setup(const glm::vec3& dam_size,
+                                             const glm::vec3& fluid_size, float spacing,
+                                             const SPHParameters& params);
+std::vector<Particle> create_fluid_drop_setup(const glm::vec3& center, float radius,
+                                              float spacing, const SPHParameters& params);
+std::vector<Particle> create_granular_flow_setup(const glm::vec3& pile_size,
+                                                 const glm::vec3& domain_size, float spacing,
+                                                 const SPHParameters& params);
+
+bool validate_particle_setup(const std::vector<Particle>& particles);
+float compute_average_neighbors(const SPHEngine& engine);
+
+}  // namespace utils
+
+}  // namespace sph

@@ -29,7 +29,9 @@ EXPORTS = (
     "sphx_version", "sphx_strerror", "sphx_create", "sphx_destroy", "sphx_set_stream",
     "sphx_set_params", "sphx_upload", "sphx_step", "sphx_eval", "sphx_download",
     "sphx_size", "sphx_get_time", "sphx_set_time", "sphx_get_stats", "sphx_reset_stats",
-    "sphx_snapshot", "sphx_restore", "sphx_debug_pairs", "sphx_density_noalloc",
+    "sphx_snapshot", "sphx_restore", "sphx_debug_pairs", "sphx_grid_create",
+    "sphx_grid_destroy", "sphx_grid_build", "sphx_grid_query", "sphx_grid_info",
+    "sphx_grid_cell", "sphx_density_noalloc",
 )
 NOALLOC_MAX_PARTICLES = 65536
 
@@ -100,6 +102,12 @@ def load_library(path: Path | str = LIB_PATH) -> C.CDLL:
         "sphx_restore": ([vp], C.c_int),
         "sphx_debug_pairs": ([vp, fp, fp, C.POINTER(sz)], C.c_int),
         "sphx_density_noalloc": ([C.POINTER(SphxParams), sz, fp, fp, fp, fp, vp], C.c_int),
+        "sphx_grid_create": ([C.POINTER(vp), sz], C.c_int),
+        "sphx_grid_destroy": ([vp], None),
+        "sphx_grid_build": ([vp, sz, fp, C.c_float], C.c_int),
+        "sphx_grid_query": ([vp, sz, fp, C.c_float, fp, fp, C.POINTER(sz)], C.c_int),
+        "sphx_grid_info": ([vp, C.POINTER(sz), C.POINTER(sz)], C.c_int),
+        "sphx_grid_cell": ([vp, C.c_int, C.c_int, C.c_int, fp, C.POINTER(sz)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -268,3 +276,60 @@ def density_noalloc(params16, n: int, pos_ptr: int, mass_ptr: int, rho_ptr: int 
                                     cv(stream_ptr))
     if rc != OK:
         raise SphxError(rc, "sphx_density_noalloc")
+
+
+class Grid:
+    """Standalone GPU spatial hash (sphx_grid_*): SpatialHash build / query_squared."""
+
+    def __init__(self, capacity: int):
+        self._lib = lib()
+        self._h = C.c_void_p()
+        rc = self._lib.sphx_grid_create(C.byref(self._h), capacity)
+        if rc != OK:
+            raise SphxError(rc, "sphx_grid_create")
+
+    def close(self):
+        if self._h:
+            self._lib.sphx_grid_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, where):
+        if rc != OK:
+            raise SphxError(rc, where)
+
+    def build(self, pos, cell_size: float):
+        pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+        self._check(self._lib.sphx_grid_build(self._h, pos.shape[0], _ptr(pos), C.c_float(cell_size)),
+                    "sphx_grid_build")
+
+    def query(self, q, radius_squared: float):
+        q = np.ascontiguousarray(q, np.float32).reshape(-1, 3)
+        nq = q.shape[0]
+        counts = np.zeros(nq, np.int64)
+        total = C.c_size_t(0)
+        self._check(self._lib.sphx_grid_query(self._h, nq, _ptr(q), C.c_float(radius_squared),
+                                               _ptr(counts), None, C.byref(total)), "sphx_grid_query")
+        idx = np.zeros(max(total.value, 1), np.int64)
+        t2 = C.c_size_t(total.value)
+        self._check(self._lib.sphx_grid_query(self._h, nq, _ptr(q), C.c_float(radius_squared),
+                                               _ptr(counts), _ptr(idx), C.byref(t2)), "sphx_grid_query")
+        return counts, idx[: t2.value]
+
+    def info(self):
+        a, b = C.c_size_t(), C.c_size_t()
+        self._check(self._lib.sphx_grid_info(self._h, C.byref(a), C.byref(b)), "sphx_grid_info")
+        return a.value, b.value
+
+    def cell(self, x: int, y: int, z: int):
+        cnt = C.c_size_t(0)
+        self._check(self._lib.sphx_grid_cell(self._h, x, y, z, None, C.byref(cnt)), "sphx_grid_cell")
+        out = np.zeros(max(cnt.value, 1), np.int64)
+        c2 = C.c_size_t(cnt.value)
+        self._check(self._lib.sphx_grid_cell(self._h, x, y, z, _ptr(out), C.byref(c2)), "sphx_grid_cell")
+        return out[: c2.value]

@@ -26,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
               "-ffp-contract=off", "-Xptxas", "-warn-spills", f"-I{REPO / 'include'}"]
 CUDA_SOURCES = ["sphx_sort.cu", "sphx_grid.cu", "sphx_passes.cu", "sphx_capi.cu",
-                "sphx_noalloc.cu"]
+                "sphx_hash.cu", "sphx_noalloc.cu"]
 
 
 def _nvcc() -> str:
@@ -75,6 +75,57 @@ def build_sphx(force: bool = False) -> Path:
     return so
 
 
+HOST_SOURCES = ["particle.cpp", "spatial_hash.cpp", "sph_engine.cpp"]
+HOST_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
+              f"-I{REPO / 'include'}", f"-I{PKG / 'host' / 'include'}",
+              "-idirafter", str(PKG / "host" / "compat")]
+
+
+def build_host(force: bool = False) -> Path:
+    """Compiles the C++17 drop-in engine (SPHEngine, ParticleSystem, SpatialHash) into
+    libsph_gb300.so, linked against libsphx.so."""
+    sphx = build_sphx(force)
+    srcs = [PKG / "host" / "src" / s for s in HOST_SOURCES]
+    deps = srcs + list((PKG / "host" / "include").glob("*.h")) + [REPO / "include" / "sphx.h", sphx]
+    so = LIB / "libsph_gb300.so"
+    if force or _stale(so, deps):
+        _run_parallel([["g++", *HOST_FLAGS, "-shared", *map(str, srcs), f"-L{LIB}", "-lsphx",
+                        "-Wl,-rpath,$ORIGIN", "-o", str(so)]])
+    return so
+
+
+def _pybind_include() -> str | None:
+    import importlib.util
+
+    spec = importlib.util.find_spec("torch")
+    if spec and spec.submodule_search_locations:
+        inc = Path(list(spec.submodule_search_locations)[0]) / "include"
+        if (inc / "pybind11" / "pybind11.h").exists():
+            return str(inc)
+    try:
+        import pybind11
+
+        return pybind11.get_include()
+    except ImportError:
+        return None
+
+
+def build_pymodule(force: bool = False) -> Path | None:
+    """Compiles the pybind11 module `sph` (the reference's Python API) into <pkg>/lib."""
+    host = build_host(force)
+    pyinc = sysconfig.get_paths()["include"]
+    pbinc = _pybind_include()
+    if not (Path(pyinc) / "Python.h").exists() or not pbinc:
+        sys.stderr.write("sph module not built: Python.h or pybind11 headers missing\n")
+        return None
+    src = PKG / "python" / "sph_module.cpp"
+    so = LIB / ("sph" + sysconfig.get_config_var("EXT_SUFFIX"))
+    if force or _stale(so, [src, host]):
+        _run_parallel([["g++", *HOST_FLAGS, "-shared", f"-I{pyinc}", f"-I{pbinc}", str(src),
+                        f"-L{LIB}", "-lsph_gb300", "-lsphx", "-Wl,-rpath,$ORIGIN", "-o", str(so)]])
+    return so
+
+
 def build_oracle(force: bool = False) -> Path:
     """Compiles the C restatement of the reference step (test infrastructure)."""
     out_dir = REPO / "oracle" / "_build"
@@ -103,6 +154,8 @@ def build_ref() -> Path | None:
 
 def build_all(force: bool = False) -> dict:
     out = {"sphx": build_sphx(force), "oracle": build_oracle(force)}
+    out["host"] = build_host(force)
+    out["sph_module"] = build_pymodule(force)
     out["ref"] = build_ref()
     return out
 

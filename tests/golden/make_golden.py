@@ -12,6 +12,9 @@ Cases (all arrays float32 unless noted, vectors as (n, 3)):
               outside the box, particles on cell faces, a zero-velocity-mass mix
   collapse    12x12x12 jittered lattice stepped 4 times at dt 1e-3 (the reference's
               dynamics degenerate after step 1: clamped walls, crowded cells)
+  scene/*     the reference's initialize_dam_break / _fluid_drop / _granular_flow particle
+              sets (default parameters): count, SHA-256 of (n, 11) float32 records
+              pos3 vel3 mass type color3, and the first 8 records
 For each case: params16, pos, vel, mass; the neighbour lists of the initial state
 (counts int64, idx int32, reference order); rho/P/acc of one field evaluation; and for
 `steps` steps of SPHEngine::step(dt) (dt > 0 fixed, dt == 0 adaptive CFL) the positions,
@@ -108,6 +111,24 @@ def main():
         out[pre + "traj_pressure"] = np.stack([t[3] for t in traj])
         out[pre + "traj_time"] = np.array([t[4] for t in traj], np.float32)
         print(f"{name}: n={n} pairs={idx.size} max|N|={counts.max()} steps={len(dts)}")
+    # the reference's own scene generators, through SPHEngine::initialize_* with default
+    # parameters: (n, 11) records pos3 vel3 mass type color3, pinned by SHA-256
+    import ctypes as C
+    import hashlib
+    L = ref.lib
+    L.ref_engine_particles.argtypes = [C.c_void_p, C.c_void_p]
+    L.ref_engine_init_scene.argtypes = [C.c_void_p, C.c_int]
+    for which, name in enumerate(("dam_break", "fluid_drop", "granular_flow")):
+        e = O.Engine(ref, 2_000_000)
+        L.ref_engine_init_scene(e.h, which)
+        n = e.size()
+        rec = np.zeros((n, 19), np.float32)
+        L.ref_engine_particles(e.h, rec.ctypes.data_as(C.c_void_p))
+        rec11 = np.ascontiguousarray(np.concatenate([rec[:, 0:6], rec[:, 11:13], rec[:, 16:19]], axis=1))
+        out[f"scene/{name}/n"] = np.array(n, np.int64)
+        out[f"scene/{name}/sha256"] = np.frombuffer(hashlib.sha256(rec11.tobytes()).digest(), np.uint8)
+        out[f"scene/{name}/first"] = rec11[:8]
+        print(f"scene {name}: n={n}")
     path = Path(__file__).with_name("sph_ref_golden.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({path.stat().st_size / 1024:.0f} KiB)")

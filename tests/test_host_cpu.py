@@ -1,0 +1,84 @@
+"""The C++ drop-in engine and its pybind11 module `sph`, host side (no GPU needed).
+
+The module must expose the reference's Python names (python/bindings.cpp:8-166) and its
+scene generators must reproduce the reference's initial conditions bit for bit (pinned
+by the SHA-256 of the reference's own initialize_* particle records in tests/golden/).
+"""
+import hashlib
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import PKG
+
+sys.path.insert(0, str(PKG / "lib"))
+
+
+@pytest.fixture(scope="module")
+def sph(built):
+    import sphx_build
+
+    sphx_build.build_host()
+    if sphx_build.build_pymodule() is None:
+        pytest.skip("Python headers or pybind11 headers missing on this machine")
+    import sph as mod
+
+    return mod
+
+
+def test_module_surface_matches_reference_bindings(sph):
+    for name in ("SPHParameters", "ParticleType", "Particle", "ParticleSystem",
+                 "PerformanceStats", "Simulator", "create_fluid_block", "create_boundary_box"):
+        assert hasattr(sph, name), name
+    for meth in ("initialize", "initialize_dam_break", "initialize_fluid_drop",
+                 "initialize_granular_flow", "add_particles", "clear_particles", "step",
+                 "run_steps", "get_particles", "get_parameters", "get_current_time",
+                 "get_step_count", "set_parameters", "set_gravity", "set_viscosity",
+                 "set_smoothing_length", "set_boundaries", "get_performance_stats",
+                 "reset_performance_stats", "compute_conservation_errors", "get_total_mass",
+                 "get_total_energy", "validate_simulation", "is_initialized", "get_positions",
+                 "get_velocities", "get_densities", "get_pressures"):
+        assert hasattr(sph.Simulator, meth), meth
+    assert sph.__version__ == "1.0.0"
+
+
+def test_parameters_defaults(sph):
+    p = sph.SPHParameters()
+    vals = (p.rest_density, p.gas_constant, p.viscosity, p.smoothing_length, p.particle_mass,
+            p.timestep, p.gravity, p.damping, p.CFL_factor, p.neighbor_search_radius)
+    want = (1000.0, 2000.0, 0.001, 0.02, 0.001, 0.001, -9.81, 0.99, 0.4, 0.04)
+    assert np.allclose(vals, want)
+    assert p.bounds == pytest.approx((-1, 1, -1, 1, -1, 1))
+
+
+def test_particle_record(sph):
+    q = sph.Particle([0.1, 0.2, 0.3], 2.0, sph.ParticleType.BOUNDARY)
+    assert (q.position.x, q.position.y, q.position.z) == pytest.approx((0.1, 0.2, 0.3))
+    assert q.mass == 2.0 and q.type == sph.ParticleType.BOUNDARY and q.id == -1
+    assert q.temperature == pytest.approx(293.15) and q.viscosity == pytest.approx(0.001)
+    d = sph.Particle()
+    assert d.mass == 1.0 and d.type == sph.ParticleType.FLUID
+
+
+def test_create_fluid_block_shape_and_rejects_bad_vectors(sph):
+    ps = sph.create_fluid_block([0, 0, 0], [0.1, 0.05, 0.02], 0.01, 1e-3)
+    assert len(ps) == 10 * 5 * 2
+    with pytest.raises(ValueError):
+        sph.create_fluid_block([0, 0], [0.1, 0.1, 0.1], 0.01)
+
+
+@pytest.mark.parametrize("scene", ["dam_break", "fluid_drop", "granular_flow"])
+def test_scene_generators_match_reference(sph, golden, scene):
+    p = sph.SPHParameters()
+    if scene == "dam_break":
+        ps = sph.create_dam_break_setup([0.4, 0.6, 0.8], [0.2, 0.4, 0.8], 0.01, p)
+    elif scene == "fluid_drop":
+        ps = sph.create_fluid_drop_setup([0.0, 0.5, 0.0], 0.1, 0.008, p)
+    else:
+        ps = sph.create_granular_flow_setup([0.3, 0.4, 0.8], [1.0, 1.0, 1.0], 0.012, p)
+    rec = np.ascontiguousarray(sph.particle_records(ps), np.float32)
+    assert rec.shape[0] == int(golden[f"scene/{scene}/n"])
+    assert np.array_equal(rec[:8].view(np.uint32), golden[f"scene/{scene}/first"].view(np.uint32))
+    digest = np.frombuffer(hashlib.sha256(rec.tobytes()).digest(), np.uint8)
+    assert np.array_equal(digest, golden[f"scene/{scene}/sha256"])
