@@ -59,6 +59,13 @@ typedef struct sphx_params {
 
 /* mode */
 #define SPHX_MODE_EXACT 0 /* reference operation order and IEEE ops: bit-identical step */
+/* Precision mode: positions stored as an integer cell (of size neighbor_search_radius)
+ * plus an FP32 in-cell offset, pair distances formed from cell differences (no bits lost
+ * far from the origin), Neumaier-compensated density and force sums, CFL timestep and
+ * current time in FP64.  Results are judged against an FP64 evaluation, not bit for bit
+ * against the reference. */
+#define SPHX_MODE_PRECISE 1
+#define SPHX_MODE_PRECISE_FP16 2 /* as PRECISE, offsets rounded to binary16 at every write */
 
 typedef struct sphx_tuning {
     int mode;              /* SPHX_MODE_* (default EXACT) */
@@ -141,6 +148,17 @@ int sphx_eval(sphx_ctx* ctx);
  * step or eval (acc is the reference's accelerations_ buffer). */
 int sphx_download(sphx_ctx* ctx, float* pos_xyz, float* vel_xyz, float* rho, float* pressure,
                   float* acc_xyz);
+
+/* Replaces the particle set from FP64 positions (host memory).  In the precision modes
+ * the cell + offset split is taken in FP64, so positions keep their bits far from the
+ * origin; in SPHX_MODE_EXACT positions are rounded to float.  Parameters must be set
+ * first (the cell size is the search radius). */
+int sphx_upload_f64(sphx_ctx* ctx, size_t n, const double* pos_xyz, const float* vel_xyz,
+                    const float* mass);
+/* Current positions in FP64 (cell * cell_size + offset in the precision modes). */
+int sphx_download_f64(sphx_ctx* ctx, double* pos_xyz);
+/* current_time_ and the last dt in FP64 (the FP64 accumulators of the precision modes). */
+int sphx_get_time_f64(sphx_ctx* ctx, double* current_time, double* last_dt);
 
 /* Number of particles currently loaded. */
 int sphx_size(sphx_ctx* ctx, size_t* n);

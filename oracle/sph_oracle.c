@@ -445,6 +445,134 @@ void orc_fields_f64(size_t n, const float* pos, const float* vel, const float* m
     free(nl);
 }
 
+/* ---- FP64 evaluation on FP64 positions -------------------------------------------------- */
+typedef struct {
+    int64_t cx, cy, cz;
+    int64_t idx;
+} cell_item;
+
+static int cmp_cell_item(const void* a, const void* b) {
+    const cell_item* x = (const cell_item*)a;
+    const cell_item* y = (const cell_item*)b;
+    if (x->cx != y->cx) return x->cx < y->cx ? -1 : 1;
+    if (x->cy != y->cy) return x->cy < y->cy ? -1 : 1;
+    if (x->cz != y->cz) return x->cz < y->cz ? -1 : 1;
+    return x->idx < y->idx ? -1 : (x->idx > y->idx);
+}
+
+/* first index in the sorted items with cell >= (x, y, z) */
+static size_t cell_lower(const cell_item* it, size_t n, int64_t x, int64_t y, int64_t z) {
+    size_t lo = 0, hi = n;
+    while (lo < hi) {
+        const size_t mid = (lo + hi) / 2;
+        const cell_item* m = &it[mid];
+        const int less = m->cx < x || (m->cx == x && (m->cy < y || (m->cy == y && m->cz < z)));
+        if (less) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+int64_t orc_fields_f64d(size_t n, const double* pos, const float* vel, const float* mass,
+                        const float* params16, double* rho, double* P, double* acc) {
+    float prm[16];
+    load_params(params16, prm);
+    const double h = prm[3], hsq = h * h, sigma = 1.0 / (M_PI * h * h * h);
+    const double r = prm[15], r2 = r * r, cs = r;
+    cell_item* it = (cell_item*)malloc((n ? n : 1) * sizeof(cell_item));
+    size_t m = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const double* p = pos + 3 * i;
+        if (!(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]))) continue;
+        it[m].cx = (int64_t)floor(p[0] / cs);
+        it[m].cy = (int64_t)floor(p[1] / cs);
+        it[m].cz = (int64_t)floor(p[2] / cs);
+        it[m].idx = (int64_t)i;
+        ++m;
+    }
+    qsort(it, m, sizeof(cell_item), cmp_cell_item);
+    int64_t* cell_of = (int64_t*)malloc((n ? n : 1) * 3 * sizeof(int64_t));
+    unsigned char* ok = (unsigned char*)calloc(n ? n : 1, 1);
+    for (size_t k = 0; k < m; ++k) {
+        const int64_t i = it[k].idx;
+        cell_of[3 * i] = it[k].cx;
+        cell_of[3 * i + 1] = it[k].cy;
+        cell_of[3 * i + 2] = it[k].cz;
+        ok[i] = 1;
+    }
+    int64_t pairs = 0;
+    /* density and pressure over the 5x5x5 stencil (covers r = cell exactly) */
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : pairs)
+    for (long long i = 0; i < (long long)n; ++i) {
+        double d = (double)mass[i] * sigma * (2.0 / 3.0);
+        if (ok[i]) {
+            const double* pi = pos + 3 * i;
+            for (int dx = -2; dx <= 2; ++dx)
+                for (int dy = -2; dy <= 2; ++dy)
+                    for (int dz = -2; dz <= 2; ++dz) {
+                        const int64_t x = cell_of[3 * i] + dx, y = cell_of[3 * i + 1] + dy,
+                                      z = cell_of[3 * i + 2] + dz;
+                        for (size_t k = cell_lower(it, m, x, y, z);
+                             k < m && it[k].cx == x && it[k].cy == y && it[k].cz == z; ++k) {
+                            const int64_t j = it[k].idx;
+                            const double* pj = pos + 3 * j;
+                            const double rx = pi[0] - pj[0], ry = pi[1] - pj[1], rz = pi[2] - pj[2];
+                            const double q2 = rx * rx + ry * ry + rz * rz;
+                            if (q2 > r2) continue;
+                            ++pairs;
+                            if (j == i) continue;
+                            d += (double)mass[j] * w3d(sigma, sqrt(q2) / h);
+                        }
+                    }
+        }
+        rho[i] = d;
+        P[i] = (double)prm[1] * (d - (double)prm[0]);
+    }
+#pragma omp parallel for schedule(dynamic, 256)
+    for (long long i = 0; i < (long long)n; ++i) {
+        double f[3] = {0, 0, 0};
+        if (ok[i]) {
+            const double* pi = pos + 3 * i;
+            for (int dx = -2; dx <= 2; ++dx)
+                for (int dy = -2; dy <= 2; ++dy)
+                    for (int dz = -2; dz <= 2; ++dz) {
+                        const int64_t x = cell_of[3 * i] + dx, y = cell_of[3 * i + 1] + dy,
+                                      z = cell_of[3 * i + 2] + dz;
+                        for (size_t k = cell_lower(it, m, x, y, z);
+                             k < m && it[k].cx == x && it[k].cy == y && it[k].cz == z; ++k) {
+                            const int64_t j = it[k].idx;
+                            if (j == i) continue;
+                            const double* pj = pos + 3 * j;
+                            const double rv[3] = {pi[0] - pj[0], pi[1] - pj[1], pi[2] - pj[2]};
+                            const double q2 = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+                            if (q2 > r2) continue;
+                            const double rl = sqrt(q2), q = rl / h;
+                            if (rl >= 1e-6) {
+                                double c = 0.0;
+                                if (q <= 1.0) c = sigma * (-2.0 * q + 1.5 * q * q);
+                                else if (q <= 2.0) c = -sigma * 0.5 * (2.0 - q) * (2.0 - q);
+                                const double s = (double)mass[j] * (P[i] + P[j]) / (2.0 * rho[j]);
+                                for (int a = 0; a < 3; ++a) f[a] -= s * c * (rv[a] / rl) / h;
+                            }
+                            double lap = 0.0;
+                            if (q <= 1.0) lap = sigma * (-2.0 + 3.0 * q) / hsq;
+                            else if (q <= 2.0) lap = sigma * (2.0 - q) / hsq;
+                            const double s = (double)mass[j] / rho[j] * (double)prm[2];
+                            for (int a = 0; a < 3; ++a)
+                                f[a] += s * ((double)vel[3 * j + a] - (double)vel[3 * i + a]) * lap;
+                        }
+                    }
+        }
+        const double mm = mass[i];
+        f[1] += (double)prm[6] * mm;
+        for (int a = 0; a < 3; ++a) acc[3 * i + a] = f[a] / mm;
+    }
+    free(it);
+    free(cell_of);
+    free(ok);
+    return pairs;
+}
+
 /* ------------------------------------------------------------------------------------ */
 /* engine                                                                                */
 /* ------------------------------------------------------------------------------------ */

@@ -38,6 +38,12 @@ void orc_fields_f64(size_t n, const float* pos, const float* vel, const float* m
                     const float* params16, double* rho, double* P, double* acc,
                     double* sum_abs);
 
+/* FP64 evaluation on FP64 positions (the truth for the precision study): neighbour sets
+ * by dot(x_i - x_j, x_i - x_j) <= r^2 in double, density/pressure/acceleration in double
+ * with the reference's formulas.  Returns the total number of (i, j) pairs. */
+int64_t orc_fields_f64d(size_t n, const double* pos, const float* vel, const float* mass,
+                        const float* params16, double* rho, double* P, double* acc);
+
 /* ---- engine: restatement of SPHEngine state and step (src/sph_engine.cpp:13-353) ---- */
 typedef struct orc_engine orc_engine;
 orc_engine* orc_engine_new(size_t capacity);

@@ -93,6 +93,8 @@ class Port(_Lib):
         super().__init__(path)
         L = self.lib
         L.orc_fields_f64.argtypes = [C.c_size_t] + [C.c_void_p] * 8
+        L.orc_fields_f64d.argtypes = [C.c_size_t] + [C.c_void_p] * 7
+        L.orc_fields_f64d.restype = C.c_int64
         L.orc_engine_get.argtypes = [C.c_void_p] + [C.c_void_p] * 5
         L.orc_engine_set_state.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_engine_last_dt.restype = C.c_float
@@ -115,6 +117,20 @@ class Port(_Lib):
         self.lib.orc_fields_f64(n, _p(pos), _p(vel), _p(mass), _p(prm), _p(rho), _p(P),
                                 _p(acc), _p(scale))
         return (rho, P, acc, scale) if want_scale else (rho, P, acc)
+
+    def fields_f64d(self, pos64, vel, mass, params16):
+        """FP64 density, pressure, acceleration on FP64 positions (sets in FP64)."""
+        pos64 = np.ascontiguousarray(pos64, np.float64).reshape(-1, 3)
+        n = pos64.shape[0]
+        vel = _f32(vel).reshape(n, 3)
+        mass = _f32(mass).reshape(n)
+        prm = _f32(params16).reshape(16)
+        rho = np.zeros(n)
+        P = np.zeros(n)
+        acc = np.zeros((n, 3))
+        pairs = self.lib.orc_fields_f64d(n, _p(pos64), _p(vel), _p(mass), _p(prm), _p(rho),
+                                         _p(P), _p(acc))
+        return rho, P, acc, pairs
 
     def threads(self) -> int:
         return self.lib.orc_max_threads()

@@ -24,9 +24,10 @@ struct sphx_ctx {
     StepConst sc{};
     Buffers b{};
     DevState* ds = nullptr;
-    float* stage = nullptr;    // 7 * capacity floats
+    float* stage = nullptr;    // 10 * capacity floats (room for FP64 positions)
     float4* snap_pos = nullptr;
     float4* snap_vel = nullptr;
+    int4* snap_cell = nullptr;
     LaunchCtx L{};
     uint64_t steps = 0;
     uint64_t queries = 0;
@@ -109,6 +110,25 @@ void fill_step_const(sphx_ctx* c) {
     s.hi[1] = p.ymax;
     s.lo[2] = p.zmin;
     s.hi[2] = p.zmax;
+    s.precise = c->tuning.mode != SPHX_MODE_EXACT;
+    s.fp16 = c->tuning.mode == SPHX_MODE_PRECISE_FP16;
+    s.cs = p.neighbor_search_radius;
+    s.cs_d = (double)p.neighbor_search_radius;
+}
+
+__global__ void k_mass_of(int n, const float4* __restrict__ pos4, float* __restrict__ mass) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        mass[i] = pos4[i].w;
+}
+
+__global__ void k_f64_to_f32(int n3, const double* __restrict__ in, float* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+
+__global__ void k_f32_to_f64(int n3, const float* __restrict__ in, double* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n3; i += gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
 }
 
 void free_all(sphx_ctx* c) {
@@ -116,7 +136,7 @@ void free_all(sphx_ctx* c) {
     void* ptrs[] = {b.pos4, b.vel4,   b.pos4_s, b.vel4_s,     b.aux4_s,    b.acc4_s,
                     b.key[0], b.key[1], b.val[0], b.val[1],   b.key_s,     b.id_s,
                     b.off,  b.tile_start, b.hist, b.scan_part, b.diag_part, c->ds,
-                    c->stage, c->snap_pos, c->snap_vel};
+                    c->stage, c->snap_pos, c->snap_vel, c->snap_cell, b.cell4, b.cell4_s};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto& slot : c->prof)
@@ -220,6 +240,10 @@ int sphx_create(sphx_ctx** out, size_t capacity, const sphx_tuning* tuning) {
     sphx_ctx* c = new (std::nothrow) sphx_ctx();
     if (!c) return SPHX_ERR_OOM;
     if (tuning) c->tuning = *tuning;
+    if (c->tuning.mode < SPHX_MODE_EXACT || c->tuning.mode > SPHX_MODE_PRECISE_FP16) {
+        delete c;
+        return SPHX_ERR_INVALID_ARG;
+    }
     if (c->tuning.warps_per_block <= 0 || c->tuning.warps_per_block > 4)
         c->tuning.warps_per_block = kDefaultWarpsPerBlock;
     int rc = SPHX_OK;
@@ -264,7 +288,10 @@ int sphx_create(sphx_ctx** out, size_t capacity, const sphx_tuning* tuning) {
         (rc = dmalloc(&b.tile_start, C)) || (rc = dmalloc(&b.hist, hist_n)) ||
         (rc = dmalloc(&b.scan_part, (size_t)b.scan_part_cap)) ||
         (rc = dmalloc(&b.diag_part, (size_t)b.diag_blocks * kDiagSums)) ||
-        (rc = dmalloc(&c->ds, 1)) || (rc = dmalloc(&c->stage, 7 * C)))
+        (rc = dmalloc(&c->ds, 1)) || (rc = dmalloc(&c->stage, 10 * C)))
+        return fail(rc);
+    if (c->tuning.mode != SPHX_MODE_EXACT &&
+        ((rc = dmalloc(&b.cell4, C)) || (rc = dmalloc(&b.cell4_s, C))))
         return fail(rc);
     if (cudaMemset(c->ds, 0, sizeof(DevState)) != cudaSuccess) return fail(SPHX_ERR_CUDA);
     if (cudaMemset(b.aux4_s, 0, C * sizeof(float4)) != cudaSuccess ||
@@ -301,6 +328,23 @@ int sphx_set_params(sphx_ctx* c, const sphx_params* p) {
     if (!p) return SPHX_ERR_INVALID_ARG;
     const float r = p->neighbor_search_radius;
     if (!(r > 0.0f) || !std::isfinite(r) || !std::isfinite(1.0f / r)) return SPHX_ERR_INVALID_ARG;
+    const bool rebin = c->b.cell4 && c->have_params && c->n > 0 &&
+                       p->neighbor_search_radius != c->params.neighbor_search_radius;
+    if (rebin) {  // precision mode: cells are sized by the search radius -- re-split
+        fill_step_const(c);
+        double* s64 = reinterpret_cast<double*>(c->stage);
+        float* s_mass = c->stage + 9 * c->capacity;
+        float* s_vel = c->stage + 6 * c->capacity;
+        launch_unpack_cells(c->L, c->sc, (int)c->n, c->b.cell4, c->b.pos4, nullptr, s64);
+        launch_unpack_state(c->L, (int)c->n, c->b.pos4, c->b.vel4, nullptr, s_vel);
+        k_mass_of<<<c->L.num_sms * 4, 256, 0, c->stream>>>((int)c->n, c->b.pos4, s_mass);
+        c->params = *p;
+        fill_step_const(c);
+        launch_pack_cells(c->L, c->sc, (int)c->n, nullptr, s64, s_vel, s_mass, c->b.cell4,
+                          c->b.pos4, c->b.vel4);
+        SPHX_CUDA(cudaGetLastError());
+        c->have_fields = false;
+    }
     c->params = *p;
     c->have_params = true;
     return SPHX_OK;
@@ -311,6 +355,7 @@ int sphx_upload(sphx_ctx* c, size_t n, const float* pos, const float* vel, const
     if (rc) return rc;
     if (n > c->capacity) return SPHX_ERR_CAPACITY;
     if (n > 0 && (!pos || !mass)) return SPHX_ERR_INVALID_ARG;
+    if (c->b.cell4 && !c->have_params) return SPHX_ERR_NOT_READY;  // cells need the cell size
     float* s_pos = c->stage;
     float* s_vel = c->stage + 3 * c->capacity;
     float* s_mass = c->stage + 6 * c->capacity;
@@ -319,7 +364,49 @@ int sphx_upload(sphx_ctx* c, size_t n, const float* pos, const float* vel, const
         if (vel)
             SPHX_CUDA(cudaMemcpyAsync(s_vel, vel, 3 * n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
         SPHX_CUDA(cudaMemcpyAsync(s_mass, mass, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-        launch_pack(c->L, (int)n, s_pos, vel ? s_vel : nullptr, s_mass, c->b.pos4, c->b.vel4);
+        if (c->b.cell4) {
+            fill_step_const(c);
+            launch_pack_cells(c->L, c->sc, (int)n, s_pos, nullptr, vel ? s_vel : nullptr, s_mass,
+                              c->b.cell4, c->b.pos4, c->b.vel4);
+        } else {
+            launch_pack(c->L, (int)n, s_pos, vel ? s_vel : nullptr, s_mass, c->b.pos4, c->b.vel4);
+        }
+        SPHX_CUDA(cudaGetLastError());
+    }
+    c->n = n;
+    c->have_fields = false;
+    return SPHX_OK;
+}
+
+int sphx_upload_f64(sphx_ctx* c, size_t n, const double* pos, const float* vel,
+                    const float* mass) {
+    int rc = enter(c);
+    if (rc) return rc;
+    if (n > c->capacity) return SPHX_ERR_CAPACITY;
+    if (n > 0 && (!pos || !mass)) return SPHX_ERR_INVALID_ARG;
+    if (c->b.cell4 && !c->have_params) return SPHX_ERR_NOT_READY;  // cells need the cell size
+    double* s_pos = reinterpret_cast<double*>(c->stage);              // 6 floats per particle
+    float* s_vel = c->stage + 6 * c->capacity;
+    float* s_mass = c->stage + 9 * c->capacity;
+    float* s_posf = c->stage + 6 * c->capacity;  // exact mode: converted positions (reuse)
+    if (n > 0) {
+        SPHX_CUDA(cudaMemcpyAsync(s_pos, pos, 3 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        SPHX_CUDA(cudaMemcpyAsync(s_mass, mass, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+        if (c->b.cell4) {
+            if (vel)
+                SPHX_CUDA(cudaMemcpyAsync(s_vel, vel, 3 * n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+            fill_step_const(c);
+            launch_pack_cells(c->L, c->sc, (int)n, nullptr, s_pos, vel ? s_vel : nullptr, s_mass,
+                              c->b.cell4, c->b.pos4, c->b.vel4);
+        } else {
+            k_f64_to_f32<<<c->L.num_sms * 4, 256, 0, c->stream>>>((int)(3 * n), s_pos, s_posf);
+            // velocities staged after the conversion, past the converted positions
+            float* s_vel2 = reinterpret_cast<float*>(s_pos);  // positions consumed above
+            SPHX_CUDA(cudaStreamSynchronize(c->stream));
+            if (vel)
+                SPHX_CUDA(cudaMemcpyAsync(s_vel2, vel, 3 * n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+            launch_pack(c->L, (int)n, s_posf, vel ? s_vel2 : nullptr, s_mass, c->b.pos4, c->b.vel4);
+        }
         SPHX_CUDA(cudaGetLastError());
     }
     c->n = n;
@@ -363,7 +450,12 @@ int sphx_download(sphx_ctx* c, float* pos, float* vel, float* rho, float* pressu
     float* s0 = c->stage;
     float* s1 = c->stage + 3 * c->capacity;
     if (pos || vel) {
-        launch_unpack_state(c->L, (int)n, c->b.pos4, c->b.vel4, pos ? s0 : nullptr, vel ? s1 : nullptr);
+        launch_unpack_state(c->L, (int)n, c->b.pos4, c->b.vel4,
+                            (pos && !c->b.cell4) ? s0 : nullptr, vel ? s1 : nullptr);
+        if (pos && c->b.cell4) {
+            fill_step_const(c);
+            launch_unpack_cells(c->L, c->sc, (int)n, c->b.cell4, c->b.pos4, s0, nullptr);
+        }
         SPHX_CUDA(cudaGetLastError());
         if (pos) SPHX_CUDA(cudaMemcpyAsync(pos, s0, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
         if (vel) SPHX_CUDA(cudaMemcpyAsync(vel, s1, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
@@ -389,6 +481,41 @@ int sphx_download(sphx_ctx* c, float* pos, float* vel, float* rho, float* pressu
     return SPHX_OK;
 }
 
+int sphx_download_f64(sphx_ctx* c, double* pos_xyz) {
+    int rc = enter(c);
+    if (rc) return rc;
+    if (!pos_xyz) return SPHX_ERR_INVALID_ARG;
+    rc = sync_status(c);
+    if (rc) return rc;
+    const size_t n = c->n;
+    if (n == 0) return SPHX_OK;
+    double* s = reinterpret_cast<double*>(c->stage);
+    if (c->b.cell4) {
+        fill_step_const(c);
+        launch_unpack_cells(c->L, c->sc, (int)n, c->b.cell4, c->b.pos4, nullptr, s);
+    } else {
+        float* sf = c->stage + 6 * c->capacity;
+        launch_unpack_state(c->L, (int)n, c->b.pos4, c->b.vel4, sf, nullptr);
+        k_f32_to_f64<<<c->L.num_sms * 4, 256, 0, c->stream>>>((int)(3 * n), sf, s);
+    }
+    SPHX_CUDA(cudaGetLastError());
+    SPHX_CUDA(cudaMemcpyAsync(pos_xyz, s, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    SPHX_CUDA(cudaStreamSynchronize(c->stream));
+    return SPHX_OK;
+}
+
+int sphx_get_time_f64(sphx_ctx* c, double* current_time, double* last_dt) {
+    int rc = enter(c);
+    if (rc) return rc;
+    SPHX_CUDA(cudaStreamSynchronize(c->stream));
+    DevState s;
+    SPHX_CUDA(cudaMemcpy(&s, c->ds, sizeof(DevState), cudaMemcpyDeviceToHost));
+    const bool p = c->tuning.mode != SPHX_MODE_EXACT;
+    if (current_time) *current_time = p ? s.time64 : (double)s.time;
+    if (last_dt) *last_dt = p ? s.dt64 : (double)s.dt;
+    return SPHX_OK;
+}
+
 int sphx_get_time(sphx_ctx* c, float* current_time, float* last_dt) {
     int rc = enter(c);
     if (rc) return rc;
@@ -406,6 +533,9 @@ int sphx_set_time(sphx_ctx* c, float t) {
     SPHX_CUDA(cudaStreamSynchronize(c->stream));
     SPHX_CUDA(cudaMemcpy(reinterpret_cast<char*>(c->ds) + offsetof(DevState, time), &t,
                          sizeof(float), cudaMemcpyHostToDevice));
+    const double t64 = t;
+    SPHX_CUDA(cudaMemcpy(reinterpret_cast<char*>(c->ds) + offsetof(DevState, time64), &t64,
+                         sizeof(double), cudaMemcpyHostToDevice));
     return SPHX_OK;
 }
 
@@ -464,10 +594,13 @@ int sphx_snapshot(sphx_ctx* c) {
     if (!c->snap_pos) {
         if ((rc = dmalloc(&c->snap_pos, c->capacity)) || (rc = dmalloc(&c->snap_vel, c->capacity)))
             return rc;
+        if (c->b.cell4 && (rc = dmalloc(&c->snap_cell, c->capacity))) return rc;
     }
     if (c->n) {
         SPHX_CUDA(cudaMemcpyAsync(c->snap_pos, c->b.pos4, c->n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
         SPHX_CUDA(cudaMemcpyAsync(c->snap_vel, c->b.vel4, c->n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
+        if (c->b.cell4)
+            SPHX_CUDA(cudaMemcpyAsync(c->snap_cell, c->b.cell4, c->n * sizeof(int4), cudaMemcpyDeviceToDevice, c->stream));
     }
     return SPHX_OK;
 }
@@ -479,6 +612,8 @@ int sphx_restore(sphx_ctx* c) {
     if (c->n) {
         SPHX_CUDA(cudaMemcpyAsync(c->b.pos4, c->snap_pos, c->n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
         SPHX_CUDA(cudaMemcpyAsync(c->b.vel4, c->snap_vel, c->n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
+        if (c->b.cell4)
+            SPHX_CUDA(cudaMemcpyAsync(c->b.cell4, c->snap_cell, c->n * sizeof(int4), cudaMemcpyDeviceToDevice, c->stream));
     }
     return SPHX_OK;
 }

@@ -33,6 +33,7 @@ __global__ void k_begin_step(DevState* ds, int reset_bbox) {
     }
     ds->nonfinite = 0;
     ds->vmax_bits = 0;
+    ds->vmax64 = 0ull;
     ds->occupied = 0;
     ds->max_occ = 0;
     ds->n_tiles = 0;
@@ -79,14 +80,51 @@ __global__ void k_set_dt(StepConst c, DevState* ds, float host_dt) {
     ds->time = xadd(ds->time, dt);
 }
 
+// Precision mode: max |v| in FP64 (NaN ignored), then the same rule in FP64; time in FP64.
+__global__ void k_vmax64(const float4* __restrict__ vel4, int n, DevState* ds) {
+    unsigned long long m = 0ull;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 v = vel4[i];
+        const double len = sqrt((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
+        if (!isnan(len)) m = max(m, (unsigned long long)__double_as_longlong(len));
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(&ds->vmax64, m);
+}
+
+__global__ void k_set_dt64(StepConst c, DevState* ds, float host_dt) {
+    if (threadIdx.x != 0) return;
+    double dt = host_dt;
+    if (host_dt <= 0.0f) {
+        const double vmax = __longlong_as_double((long long)ds->vmax64);
+        const double cfl = c.cfl, h = c.h;
+        const double dt_cfl = cfl * h / (vmax + 1e-6);
+        const double a0 = sqrt((double)ds->a0[0] * ds->a0[0] + (double)ds->a0[1] * ds->a0[1] +
+                               (double)ds->a0[2] * ds->a0[2]);
+        const double dt_force = cfl * sqrt(h / (a0 + 1e-6));
+        dt = dt_cfl;
+        if (dt_force < dt) dt = dt_force;
+        if ((double)c.timestep < dt) dt = c.timestep;
+    }
+    ds->dt64 = dt;
+    ds->time64 += dt;
+    ds->dt = (float)dt;
+    ds->time = (float)ds->time64;
+}
+
 int launch_cfl(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds,
                float host_dt) {
     int launches = 1;
     if (host_dt <= 0.0f) {
-        k_vmax<<<grid_blocks(L, c.n, 256), 256, 0, L.stream>>>(b.vel4, c.n, ds);
+        if (c.precise)
+            k_vmax64<<<grid_blocks(L, c.n, 256), 256, 0, L.stream>>>(b.vel4, c.n, ds);
+        else
+            k_vmax<<<grid_blocks(L, c.n, 256), 256, 0, L.stream>>>(b.vel4, c.n, ds);
         ++launches;
     }
-    k_set_dt<<<1, 32, 0, L.stream>>>(c, ds, host_dt);
+    if (c.precise) k_set_dt64<<<1, 32, 0, L.stream>>>(c, ds, host_dt);
+    else k_set_dt<<<1, 32, 0, L.stream>>>(c, ds, host_dt);
     return launches;
 }
 
@@ -135,6 +173,57 @@ __global__ void k_bbox(const float4* __restrict__ pos4, int n, float inv_cell, D
 // that fold onto each other are at least F - 2 cells apart, so a candidate from a folded
 // neighbour fails the distance test; sets and visiting order are unchanged, only the
 // number of candidates grows.
+// Precision mode: the cells are stored; w != 0 marks a particle with no finite position.
+__global__ void k_bbox_cells(const int4* __restrict__ cell4, int n, DevState* ds) {
+    int mn[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff};
+    int mx[3] = {-0x7fffffff - 1, -0x7fffffff - 1, -0x7fffffff - 1};
+    uint32_t bad = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int4 c = cell4[i];
+        if (c.w) {
+            ++bad;
+            continue;
+        }
+        mn[0] = min(mn[0], c.x); mn[1] = min(mn[1], c.y); mn[2] = min(mn[2], c.z);
+        mx[0] = max(mx[0], c.x); mx[1] = max(mx[1], c.y); mx[2] = max(mx[2], c.z);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = min(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+            mx[a] = max(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+        }
+        bad += __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            if (mn[a] != 0x7fffffff) atomicMin(&ds->cmin[a], mn[a]);
+            if (mx[a] != -0x7fffffff - 1) atomicMax(&ds->cmax[a], mx[a]);
+        }
+        if (bad) atomicAdd(&ds->nonfinite, bad);
+    }
+}
+
+__global__ void k_keys_cells(const int4* __restrict__ cell4, int n, const DevState* ds,
+                             uint32_t* __restrict__ keys) {
+    if (ds->status) return;
+    const int cx0 = ds->cmin[0], cy0 = ds->cmin[1], cz0 = ds->cmin[2];
+    const uint32_t dx = ds->dim[0], dy = ds->dim[1], dz = ds->dim[2], nc = ds->ncells;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int4 c = cell4[i];
+        uint32_t key = nc;
+        if (!c.w) {
+            const uint32_t x = (uint32_t)(c.x - cx0) % dx;
+            const uint32_t y = (uint32_t)(c.y - cy0) % dy;
+            const uint32_t z = (uint32_t)(c.z - cz0) % dz;
+            key = (x * dy + y) * dz + z;
+        }
+        keys[i] = key;
+    }
+}
+
 __global__ void k_grid_setup(int n, uint32_t max_cells, DevState* ds) {
     if (threadIdx.x != 0) return;
     if ((int)ds->nonfinite >= n) {  // no finite particle: a one-cell grid, all keys sentinel
@@ -202,6 +291,7 @@ __global__ void k_reorder(const Buffers b, int n, DevState* ds) {
         b.id_s[k] = id;
         b.pos4_s[k] = b.pos4[id];
         b.vel4_s[k] = b.vel4[id];
+        if (b.cell4) b.cell4_s[k] = b.cell4[id];
     }
 }
 
@@ -222,9 +312,11 @@ int launch_build_grid(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                       DevState* ds) {
     const int n = c.n;
     const int gb = grid_blocks(L, n, 256);
-    k_bbox<<<gb, 256, 0, L.stream>>>(b.pos4, n, c.inv_cell, ds);
+    if (c.precise) k_bbox_cells<<<gb, 256, 0, L.stream>>>(b.cell4, n, ds);
+    else k_bbox<<<gb, 256, 0, L.stream>>>(b.pos4, n, c.inv_cell, ds);
     k_grid_setup<<<1, 32, 0, L.stream>>>(n, c.max_cells, ds);
-    k_keys<<<gb, 256, 0, L.stream>>>(b.pos4, n, c.inv_cell, ds, b.key[0]);
+    if (c.precise) k_keys_cells<<<gb, 256, 0, L.stream>>>(b.cell4, n, ds, b.key[0]);
+    else k_keys<<<gb, 256, 0, L.stream>>>(b.pos4, n, c.inv_cell, ds, b.key[0]);
     const int r = launch_radix_sort(L, b, ds, n);
     k_reorder<<<grid_blocks(L, n, 256, 8), 256, 0, L.stream>>>(b, n, ds);
     k_offsets<<<grid_blocks(L, n + 1, 256, 8), 256, 0, L.stream>>>(b.key_s, n, ds, b.off);
@@ -236,7 +328,8 @@ int launch_build_grid(const LaunchCtx& L, const StepConst& c, const Buffers& b,
 // Fixed partition and fixed-order final sum: bit-reproducible run to run.
 __global__ void __launch_bounds__(kDiagThreads) k_diag_partial(
     const float4* __restrict__ pos4, const float4* __restrict__ vel4,
-    const float4* __restrict__ aux4_s, int n, float grav, double* __restrict__ part) {
+    const float4* __restrict__ aux4_s, const int4* __restrict__ cell4, double cs, int n,
+    float grav, double* __restrict__ part) {
     double s[7] = {0, 0, 0, 0, 0, 0, 0};
     const int per = (n + gridDim.x - 1) / gridDim.x;
     const int i0 = blockIdx.x * per, i1 = min(n, i0 + per);
@@ -249,7 +342,8 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_partial(
         s[2] += m * v.y;
         s[3] += m * v.z;
         s[4] += 0.5 * m * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
-        s[5] += -m * (double)grav * (double)p.y;
+        const double y = cell4 ? (double)cell4[i].y * cs + (double)p.y : (double)p.y;
+        s[5] += -m * (double)grav * y;
         s[6] += (double)aux4_s[i].x;
     }
     __shared__ double red[kDiagThreads / 32][7];
@@ -277,8 +371,8 @@ __global__ void k_diag_final(const double* __restrict__ part, int nb, DevState* 
 }
 
 int launch_diag(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds) {
-    k_diag_partial<<<b.diag_blocks, kDiagThreads, 0, L.stream>>>(b.pos4, b.vel4, b.aux4_s, c.n,
-                                                                 c.grav, b.diag_part);
+    k_diag_partial<<<b.diag_blocks, kDiagThreads, 0, L.stream>>>(
+        b.pos4, b.vel4, b.aux4_s, c.precise ? b.cell4 : nullptr, c.cs_d, c.n, c.grav, b.diag_part);
     k_diag_final<<<1, 32, 0, L.stream>>>(b.diag_part, b.diag_blocks, ds);
     return 2;
 }
@@ -346,6 +440,83 @@ void launch_unpack_sorted(const LaunchCtx& L, int n, const uint32_t* id_s, const
                           const float4* acc4_s, float* rho, float* pressure, float* acc3) {
     k_unpack_sorted<<<grid_blocks(L, n, 256, 8), 256, 0, L.stream>>>(n, id_s, aux4_s, acc4_s,
                                                                      rho, pressure, acc3);
+}
+
+}  // namespace sphx
+
+namespace sphx {
+
+// Absolute position (double) -> integer cell + offset in [0, cs); non-finite -> w = 1.
+__device__ __forceinline__ void to_cell(double X, double cs, int fp16, int& c, float& o) {
+    double f = floor(X / cs);
+    f = fmin(fmax(f, -(double)kCellClamp), (double)(kCellClamp - 1));
+    c = (int)f;
+    o = (float)(X - (double)c * cs);
+    if (fp16) o = round_half(o);
+    const float csf = (float)cs;
+    if (o >= csf) {  // rounding reached the next cell
+        o = 0.0f;
+        c += 1;
+    } else if (o < 0.0f) {
+        o = 0.0f;
+    }
+}
+
+__global__ void k_pack_cells(StepConst c, int n, const float* __restrict__ pos3f,
+                             const double* __restrict__ pos3d, const float* __restrict__ vel3,
+                             const float* __restrict__ mass, int4* __restrict__ cell4,
+                             float4* __restrict__ pos4, float4* __restrict__ vel4) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double X[3];
+        for (int a = 0; a < 3; ++a) X[a] = pos3d ? pos3d[3 * i + a] : (double)pos3f[3 * i + a];
+        int4 cc = make_int4(0, 0, 0, 0);
+        float o[3] = {0.0f, 0.0f, 0.0f};
+        if (isfinite(X[0]) && isfinite(X[1]) && isfinite(X[2])) {
+            to_cell(X[0], c.cs_d, c.fp16, cc.x, o[0]);
+            to_cell(X[1], c.cs_d, c.fp16, cc.y, o[1]);
+            to_cell(X[2], c.cs_d, c.fp16, cc.z, o[2]);
+        } else {
+            cc.w = 1;
+            for (int a = 0; a < 3; ++a) o[a] = (float)X[a];
+        }
+        cell4[i] = cc;
+        pos4[i] = make_float4(o[0], o[1], o[2], mass[i]);
+        vel4[i] = vel3 ? make_float4(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2], 0.0f)
+                       : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+}
+
+void launch_pack_cells(const LaunchCtx& L, const StepConst& c, int n, const float* pos3f,
+                       const double* pos3d, const float* vel3, const float* mass, int4* cell4,
+                       float4* pos4, float4* vel4) {
+    k_pack_cells<<<grid_blocks(L, n, 256, 8), 256, 0, L.stream>>>(c, n, pos3f, pos3d, vel3, mass,
+                                                                  cell4, pos4, vel4);
+}
+
+__global__ void k_unpack_cells(StepConst c, int n, const int4* __restrict__ cell4,
+                               const float4* __restrict__ pos4, float* __restrict__ pos3f,
+                               double* __restrict__ pos3d) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int4 cc = cell4[i];
+        const float4 p = pos4[i];
+        double X[3];
+        if (cc.w) {
+            X[0] = p.x; X[1] = p.y; X[2] = p.z;
+        } else {
+            X[0] = (double)cc.x * c.cs_d + (double)p.x;
+            X[1] = (double)cc.y * c.cs_d + (double)p.y;
+            X[2] = (double)cc.z * c.cs_d + (double)p.z;
+        }
+        for (int a = 0; a < 3; ++a) {
+            if (pos3d) pos3d[3 * i + a] = X[a];
+            if (pos3f) pos3f[3 * i + a] = (float)X[a];
+        }
+    }
+}
+
+void launch_unpack_cells(const LaunchCtx& L, const StepConst& c, int n, const int4* cell4,
+                         const float4* pos4, float* pos3f, double* pos3d) {
+    k_unpack_cells<<<grid_blocks(L, n, 256, 8), 256, 0, L.stream>>>(c, n, cell4, pos4, pos3f, pos3d);
 }
 
 }  // namespace sphx

@@ -1,6 +1,7 @@
 // Internal declarations of the sm_103a SPH step: device-resident state, per-step
 // constants, exact-arithmetic helpers and the launch wrappers shared by the .cu files.
 #pragma once
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -35,6 +36,11 @@ struct StepConst {
     float rest, gas, visc, grav, damping, cfl, timestep;
     float lo[3], hi[3];    // box
     uint32_t max_cells;    // capacity of the dense cell grid
+    // precision mode (positions = integer cell + FP32 in-cell offset)
+    int precise;           // 1: cell + offset storage, compensated sums, FP64 CFL/time
+    int fp16;              // 1: offsets rounded to binary16 at every write
+    float cs;              // cell size of the storage and of the search grid (= r_search)
+    double cs_d;           // the same, as double
 };
 
 // Device-resident scalars written and read by the kernels of a step.
@@ -56,6 +62,8 @@ struct DevState {
     float a0[4];                // accelerations_[0] (persists across steps)
     unsigned long long max_nn;  // max |N(i)| since the last stats reset
     double sums[kDiagSums];     // FP64 diagnostics of the state after the last step
+    double dt64, time64;        // precision mode: dt and current time in FP64
+    unsigned long long vmax64;  // precision mode: max |v| (FP64 bits)
 };
 
 struct Buffers {
@@ -65,6 +73,8 @@ struct Buffers {
     float4* vel4_s;
     float4* aux4_s;   // cell-sorted: rho, P, 2*rho, mass/rho
     float4* acc4_s;   // cell-sorted accelerations of the last step/eval
+    int4* cell4;      // precision mode, insertion order: cell (x, y, z), w = 1 if not finite
+    int4* cell4_s;    // precision mode, cell-sorted copy
     uint32_t* key[2]; // radix ping-pong
     uint32_t* val[2];
     uint32_t* key_s;  // sorted cell keys
@@ -144,6 +154,22 @@ __device__ __forceinline__ int cell_coord(float x, float inv_cell) {
     return (int)f;
 }
 
+// ---- precision mode helpers ----------------------------------------------------------
+
+// Neumaier's compensated summation (Neumaier 1974): sum + running correction.
+struct KSum {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        const float t = s + x;
+        if (fabsf(s) >= fabsf(x)) c += (s - t) + x;
+        else c += (x - t) + s;
+        s = t;
+    }
+    __device__ __forceinline__ float value() const { return s + c; }
+};
+
+__device__ __forceinline__ float round_half(float x) { return __half2float(__float2half_rn(x)); }
+
 // ---- launch wrappers (host) --------------------------------------------------------
 struct LaunchCtx {
     cudaStream_t stream;
@@ -178,5 +204,11 @@ void launch_unpack_state(const LaunchCtx& L, int n, const float4* pos4, const fl
 void launch_unpack_sorted(const LaunchCtx& L, int n, const uint32_t* id_s,
                           const float4* aux4_s, const float4* acc4_s, float* rho,
                           float* pressure, float* acc3);
+// precision mode: absolute positions (float or double) <-> cell + offset
+void launch_pack_cells(const LaunchCtx& L, const StepConst& c, int n, const float* pos3f,
+                       const double* pos3d, const float* vel3, const float* mass, int4* cell4,
+                       float4* pos4, float4* vel4);
+void launch_unpack_cells(const LaunchCtx& L, const StepConst& c, int n, const int4* cell4,
+                         const float4* pos4, float* pos3f, double* pos3d);
 
 }  // namespace sphx

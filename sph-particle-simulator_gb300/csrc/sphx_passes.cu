@@ -63,6 +63,50 @@ __device__ __forceinline__ void tile_setup(const StepConst& c, const Buffers& b,
     }
 }
 
+// Precision mode: the tile's frame is the cell of its first particle; a position inside
+// the frame is (cell - frame) * cs + offset, exact to a few ulps of the cell size however
+// far the frame lies from the origin.
+__device__ __forceinline__ float4 frame_pos(const int4& cell, const int4& frame, const float4& o,
+                                            float cs) {
+    return make_float4((float)(cell.x - frame.x) * cs + o.x, (float)(cell.y - frame.y) * cs + o.y,
+                       (float)(cell.z - frame.z) * cs + o.z, o.w);
+}
+
+__device__ __forceinline__ void tile_setup_cells(const StepConst& c, const Buffers& b,
+                                                 const DevState* ds, uint32_t t, int lane,
+                                                 Tile& T, float4& xi, bool& valid,
+                                                 int4& frame) {
+    const uint32_t k0 = b.tile_start[t];
+    const uint32_t key = b.key_s[k0];
+    const uint32_t nc = ds->ncells;
+    const uint32_t end = b.off[key + 1];
+    T.k0 = (int)k0;
+    T.cnt = (int)min(end - k0, (uint32_t)kTile);
+    valid = lane < T.cnt;
+    frame = b.cell4_s[k0];
+    const float4 o = valid ? b.pos4_s[k0 + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int4 ci = valid ? b.cell4_s[k0 + lane] : frame;
+    xi = frame_pos(ci, frame, o, c.cs);
+    T.cells = key < nc;
+    if (!T.cells) {
+        xi = o;
+        return;
+    }
+    const uint32_t dz = ds->dim[2], dy = ds->dim[1];
+    T.cz = (int)(key % dz);
+    T.cy = (int)((key / dz) % dy);
+    T.cx = (int)(key / (dz * dy));
+    const float off[3] = {o.x, o.y, o.z};
+    const float eps = c.cs * 2.44140625e-4f;  // 2^-12 cells
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const bool near_lo = valid && off[a] < eps;
+        const bool near_hi = valid && (c.cs - off[a]) < eps;
+        T.lo[a] = __any_sync(0xffffffffu, near_lo) ? -2 : -1;
+        T.hi[a] = __any_sync(0xffffffffu, near_hi) ? 2 : 1;
+    }
+}
+
 // Calls f(begin, end) for every stencil row of the tile, in the reference's order.  On a
 // folded axis the neighbour index wraps; a row that wraps on z is two segments, visited
 // in dz order.
@@ -189,17 +233,37 @@ __device__ __forceinline__ bool box_near(const TileBox& B, const float4& p, floa
 }
 
 // Hit mask of this lane's particle against the staged chunk (candidates in `surv` only).
+// Exact mode: the reference's rounded test; precision mode: contracted FP32 on
+// frame-relative coordinates.
+template <bool kPrecise>
 __device__ __forceinline__ uint32_t chunk_hits(const float4* cand, uint32_t surv,
                                                const float4& xi, float r2) {
     uint32_t mask = 0;
 #pragma unroll
     for (int jj = 0; jj < 32; ++jj) {
         if (surv & (1u << jj)) {
-            const Diff d = diff(xi, cand[jj]);
-            if (d.d2 <= r2) mask |= 1u << jj;
+            float d2;
+            if (kPrecise) {
+                const float4 xj = cand[jj];
+                const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+                d2 = dx * dx + dy * dy + dz * dz;
+            } else {
+                d2 = diff(xi, cand[jj]).d2;
+            }
+            if (d2 <= r2) mask |= 1u << jj;
         }
     }
     return mask;
+}
+
+// W(q) in precision mode (same formula, contracted arithmetic)
+__device__ __forceinline__ float cubic_w_p(const StepConst& c, float q) {
+    if (q <= 1.0f) return c.sigma * (2.0f / 3.0f - q * q + 0.5f * q * q * q);
+    if (q <= 2.0f) {
+        const float t = 2.0f - q;
+        return c.sigma * (t * t * t * (1.0f / 6.0f));
+    }
+    return 0.0f;
 }
 
 // Work distribution: warps take tiles from a per-pass counter (dynamic, so crowded cells
@@ -222,7 +286,8 @@ struct DensitySmem {
     float tbuf[kDensityBatch];
 };
 
-__global__ void __launch_bounds__(128) k_density(const StepConst c, const Buffers b,
+template <bool kPrecise>
+__global__ void __launch_bounds__(128, 8) k_density(const StepConst c, const Buffers b,
                                                  DevState* ds) {
     if (ds->status) return;
     extern __shared__ __align__(16) unsigned char smem_raw_d[];
@@ -236,22 +301,27 @@ __global__ void __launch_bounds__(128) k_density(const StepConst c, const Buffer
         Tile T;
         float4 xi;
         bool valid;
-        tile_setup(c, b, ds, t, lane, T, xi, valid);
+        int4 frame = make_int4(0, 0, 0, 0);
+        if (kPrecise) tile_setup_cells(c, b, ds, t, lane, T, xi, valid, frame);
+        else tile_setup(c, b, ds, t, lane, T, xi, valid);
         const int i = T.k0 + lane;
         const TileBox B = tile_box(xi, valid);
         S->tpos[lane] = xi;
         float rho = xmul(xi.w, c.w0);
+        KSum rk;
+        rk.s = rho;
         uint32_t nn = 0;
         for_each_row(b, ds, T, [&](int a, int e) {
             for (int s = a; s < e; s += kTile) {
                 const int m = min(kTile, e - s);
                 __syncwarp();
-                const float4 pl = lane < m ? b.pos4_s[s + lane] : make_float4(inf, inf, inf, 0.f);
+                float4 pl = lane < m ? b.pos4_s[s + lane] : make_float4(inf, inf, inf, 0.f);
+                if (kPrecise && lane < m) pl = frame_pos(b.cell4_s[s + lane], frame, pl, c.cs);
                 S->cand[lane] = pl;
                 const uint32_t surv = __ballot_sync(kFull, box_near(B, pl, r2m));
                 __syncwarp();
                 if (!surv) continue;
-                uint32_t mask = valid ? chunk_hits(S->cand, surv, xi, c.r2) : 0u;
+                uint32_t mask = valid ? chunk_hits<kPrecise>(S->cand, surv, xi, c.r2) : 0u;
                 nn += __popc(mask);
                 const int self = i - s;
                 if ((unsigned)self < 32u) mask &= ~(1u << self);
@@ -267,18 +337,29 @@ __global__ void __launch_bounds__(128) k_density(const StepConst c, const Buffer
                     for (uint32_t f = base + lane; f < end; f += 32) {
                         const uint32_t pr = S->plist[f];
                         const float4 xj = S->cand[pr & 31];
-                        const Diff d = diff(S->tpos[pr >> 5], xj);
-                        const float q = xdiv(xsqrt(d.d2), c.h);
-                        S->tbuf[f - base] = xmul(xj.w, cubic_w(c, q));
+                        if (kPrecise) {
+                            const float4 xt = S->tpos[pr >> 5];
+                            const float dx = xt.x - xj.x, dy = xt.y - xj.y, dz = xt.z - xj.z;
+                            const float q = sqrtf(dx * dx + dy * dy + dz * dz) / c.h;
+                            S->tbuf[f - base] = xj.w * cubic_w_p(c, q);
+                        } else {
+                            const Diff d = diff(S->tpos[pr >> 5], xj);
+                            const float q = xdiv(xsqrt(d.d2), c.h);
+                            S->tbuf[f - base] = xmul(xj.w, cubic_w(c, q));
+                        }
                     }
                     __syncwarp();
                     const uint32_t k1 = min(o + cnt, end);
-                    for (uint32_t k = max(o, base); k < k1; ++k) rho = xadd(rho, S->tbuf[k - base]);
+                    if (kPrecise)
+                        for (uint32_t k = max(o, base); k < k1; ++k) rk.add(S->tbuf[k - base]);
+                    else
+                        for (uint32_t k = max(o, base); k < k1; ++k) rho = xadd(rho, S->tbuf[k - base]);
                     __syncwarp();
                 }
             }
         });
         if (valid) {
+            if (kPrecise) rho = rk.value();
             const float P = xmul(c.gas, xsub(rho, c.rest));
             b.aux4_s[i] = make_float4(rho, P, xmul(2.0f, rho), xdiv(xi.w, rho));
             my_max = max(my_max, nn);
@@ -339,7 +420,75 @@ __device__ __forceinline__ void force_term(const StepConst& c, const float4& xt,
     v3[2] = xmul(xmul(sv, xsub(vj.z, vt.z)), lap);
 }
 
-template <bool kIntegrate>
+// Precision-mode pair term: the same formulas with contracted FP32 arithmetic.
+__device__ __forceinline__ void force_term_p(const StepConst& c, const float4& xt,
+                                             const float4& vt, float Pt, const float4& xj,
+                                             const float4& vj, const float4& aj, float* p3,
+                                             float* v3, bool& skip) {
+    const float dx = xt.x - xj.x, dy = xt.y - xj.y, dz = xt.z - xj.z;
+    const float r_len = sqrtf(dx * dx + dy * dy + dz * dz);
+    const float q = r_len / c.h;
+    skip = r_len < 1e-6f;
+    p3[0] = p3[1] = p3[2] = 0.0f;
+    if (!skip) {
+        float gf = 0.0f;
+        if (q <= 1.0f) gf = c.sigma * (-2.0f * q + 1.5f * q * q);
+        else if (q <= 2.0f) gf = -c.sigma * 0.5f * (2.0f - q) * (2.0f - q);
+        const float s = xj.w * (Pt + aj.y) / aj.z * gf / (r_len * c.h);
+        p3[0] = s * dx;
+        p3[1] = s * dy;
+        p3[2] = s * dz;
+    }
+    float lap = 0.0f;
+    if (q <= 1.0f) lap = c.sigma * (-2.0f + 3.0f * q) / c.h_sq;
+    else if (q <= 2.0f) lap = c.sigma * (2.0f - q) / c.h_sq;
+    const float sv = aj.w * c.visc * lap;
+    v3[0] = sv * (vj.x - vt.x);
+    v3[1] = sv * (vj.y - vt.y);
+    v3[2] = sv * (vj.z - vt.z);
+}
+
+// Precision-mode leapfrog + wall clamp on cell + offset positions (FP64 clamp).
+__device__ __forceinline__ void integrate_cells(const StepConst& c, float dt, const float* acc,
+                                                float* o, float* v, int4& cell) {
+    int* cc[3] = {&cell.x, &cell.y, &cell.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float half = 0.5f * acc[a] * dt;
+        float vv = v[a] + half;
+        float on = o[a] + vv * dt;
+        vv = vv + half;
+        v[a] = vv * c.damping;
+        if (!isfinite(on)) {  // the position is lost: park the particle as non-finite
+            cell.w = 1;
+            o[a] = on;
+            continue;
+        }
+        double X = (double)(*cc[a]) * c.cs_d + (double)on;
+        if (X < (double)c.lo[a]) {
+            X = c.lo[a];
+            v[a] = v[a] * -0.8f;
+        } else if (X > (double)c.hi[a]) {
+            X = c.hi[a];
+            v[a] = v[a] * -0.8f;
+        }
+        double f = floor(X / c.cs_d);
+        f = fmin(fmax(f, -(double)kCellClamp), (double)(kCellClamp - 1));
+        int ci = (int)f;
+        float oo = (float)(X - (double)ci * c.cs_d);
+        if (c.fp16) oo = round_half(oo);
+        if (oo >= c.cs) {
+            oo = 0.0f;
+            ci += 1;
+        } else if (oo < 0.0f) {
+            oo = 0.0f;
+        }
+        *cc[a] = ci;
+        o[a] = oo;
+    }
+}
+
+template <bool kIntegrate, bool kPrecise>
 __global__ void __launch_bounds__(128, 6) k_force(const StepConst c, const Buffers b,
                                                DevState* ds) {
     if (ds->status) return;
@@ -354,7 +503,9 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst c, const Buffe
         Tile T;
         float4 xi;
         bool valid;
-        tile_setup(c, b, ds, t, lane, T, xi, valid);
+        int4 frame = make_int4(0, 0, 0, 0);
+        if (kPrecise) tile_setup_cells(c, b, ds, t, lane, T, xi, valid, frame);
+        else tile_setup(c, b, ds, t, lane, T, xi, valid);
         const int i = T.k0 + lane;
         const float4 vi = valid ? b.vel4_s[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float Pi = valid ? b.aux4_s[i].y : 0.0f;
@@ -364,12 +515,14 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst c, const Buffe
         S->tP[lane] = Pi;
         float fpx = 0.0f, fpy = 0.0f, fpz = 0.0f;
         float fvx = 0.0f, fvy = 0.0f, fvz = 0.0f;
+        KSum Fx, Fy, Fz;  // precision mode: one compensated sum per component
         for_each_row(b, ds, T, [&](int a, int e) {
             for (int s = a; s < e; s += kTile) {
                 const int m = min(kTile, e - s);
                 __syncwarp();
                 const bool in = lane < m;
-                const float4 pl = in ? b.pos4_s[s + lane] : make_float4(inf, inf, inf, 0.f);
+                float4 pl = in ? b.pos4_s[s + lane] : make_float4(inf, inf, inf, 0.f);
+                if (kPrecise && in) pl = frame_pos(b.cell4_s[s + lane], frame, pl, c.cs);
                 S->cpos[lane] = pl;
                 const uint32_t surv = __ballot_sync(kFull, box_near(B, pl, r2m));
                 if (!surv) continue;
@@ -378,7 +531,7 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst c, const Buffe
                     S->caux[lane] = b.aux4_s[s + lane];
                 }
                 __syncwarp();
-                uint32_t mask = valid ? chunk_hits(S->cpos, surv, xi, c.r2) : 0u;
+                uint32_t mask = valid ? chunk_hits<kPrecise>(S->cpos, surv, xi, c.r2) : 0u;
                 const int self = i - s;
                 if ((unsigned)self < 32u) mask &= ~(1u << self);
                 const uint32_t cnt = __popc(mask);
@@ -395,8 +548,12 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst c, const Buffe
                         const int tt = pr >> 5, jj = pr & 31;
                         float p3[3], v3[3];
                         bool sk;
-                        force_term(c, S->tpos[tt], S->tvel[tt], S->tP[tt], S->cpos[jj],
-                                   S->cvel[jj], S->caux[jj], p3, v3, sk);
+                        if (kPrecise)
+                            force_term_p(c, S->tpos[tt], S->tvel[tt], S->tP[tt], S->cpos[jj],
+                                         S->cvel[jj], S->caux[jj], p3, v3, sk);
+                        else
+                            force_term(c, S->tpos[tt], S->tvel[tt], S->tP[tt], S->cpos[jj],
+                                       S->cvel[jj], S->caux[jj], p3, v3, sk);
                         const uint32_t u = f - base;
                         S->tb[0][u] = p3[0];
                         S->tb[1][u] = p3[1];
@@ -410,6 +567,12 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst c, const Buffe
                     const uint32_t k1 = min(o + cnt, end);
                     for (uint32_t k = max(o, base); k < k1; ++k) {
                         const uint32_t u = k - base;
+                        if (kPrecise) {
+                            Fx.add(S->tb[3][u] - S->tb[0][u]);
+                            Fy.add(S->tb[4][u] - S->tb[1][u]);
+                            Fz.add(S->tb[5][u] - S->tb[2][u]);
+                            continue;
+                        }
                         if (!S->skip[u]) {
                             fpx = xsub(fpx, S->tb[0][u]);
                             fpy = xsub(fpy, S->tb[1][u]);
@@ -426,12 +589,35 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst c, const Buffe
         __syncwarp();
         if (!valid) continue;
         const float mi = xi.w;
-        const float ax = xdiv(xadd(xadd(fpx, fvx), xmul(0.0f, mi)), mi);
-        const float ay = xdiv(xadd(xadd(fpy, fvy), xmul(c.grav, mi)), mi);
-        const float az = xdiv(xadd(xadd(fpz, fvz), xmul(0.0f, mi)), mi);
+        float ax, ay, az;
+        if (kPrecise) {
+            ax = Fx.value() / mi;
+            ay = (Fy.value() + c.grav * mi) / mi;
+            az = Fz.value() / mi;
+        } else {
+            ax = xdiv(xadd(xadd(fpx, fvx), xmul(0.0f, mi)), mi);
+            ay = xdiv(xadd(xadd(fpy, fvy), xmul(c.grav, mi)), mi);
+            az = xdiv(xadd(xadd(fpz, fvz), xmul(0.0f, mi)), mi);
+        }
         b.acc4_s[i] = make_float4(ax, ay, az, 0.0f);
         if (!kIntegrate) continue;
         const uint32_t id = b.id_s[i];
+        if (kPrecise) {
+            int4 cell = b.cell4_s[i];
+            const float4 own = b.pos4_s[i];
+            float o[3] = {own.x, own.y, own.z}, v[3] = {vi.x, vi.y, vi.z};
+            const float acc[3] = {ax, ay, az};
+            if (!cell.w) integrate_cells(c, dt, acc, o, v, cell);
+            b.cell4[id] = cell;
+            b.pos4[id] = make_float4(o[0], o[1], o[2], mi);
+            b.vel4[id] = make_float4(v[0], v[1], v[2], 0.0f);
+            if (id == 0) {
+                ds->a0[0] = ax;
+                ds->a0[1] = ay;
+                ds->a0[2] = az;
+            }
+            continue;
+        }
         float x[3] = {xi.x, xi.y, xi.z}, v[3] = {vi.x, vi.y, vi.z};
         const float acc[3] = {ax, ay, az};
 #pragma unroll
@@ -462,7 +648,7 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst c, const Buffe
 // ---------------------------------------------------------------------------------------
 // neighbour-list dump (test hook): same walk, lists written in iteration order
 // ---------------------------------------------------------------------------------------
-template <bool kFill>
+template <bool kFill, bool kPrecise>
 __global__ void __launch_bounds__(128) k_pairs(const StepConst c, const Buffers b,
                                                const DevState* ds, uint32_t* counts_by_id,
                                                const uint64_t* off_by_id, int64_t* out) {
@@ -476,7 +662,9 @@ __global__ void __launch_bounds__(128) k_pairs(const StepConst c, const Buffers 
         Tile T;
         float4 xi;
         bool valid;
-        tile_setup(c, b, ds, t, lane, T, xi, valid);
+        int4 frame = make_int4(0, 0, 0, 0);
+        if (kPrecise) tile_setup_cells(c, b, ds, t, lane, T, xi, valid, frame);
+        else tile_setup(c, b, ds, t, lane, T, xi, valid);
         const int i = T.k0 + lane;
         const uint32_t id = valid ? b.id_s[i] : 0u;
         uint64_t pos = (kFill && valid) ? off_by_id[id] : 0ull;
@@ -485,11 +673,22 @@ __global__ void __launch_bounds__(128) k_pairs(const StepConst c, const Buffers 
             for (int s = a; s < e; s += kTile) {
                 const int m = min(kTile, e - s);
                 __syncwarp();
-                if (lane < m) cand[lane] = b.pos4_s[s + lane];
+                if (lane < m) {
+                    float4 p = b.pos4_s[s + lane];
+                    if (kPrecise) p = frame_pos(b.cell4_s[s + lane], frame, p, c.cs);
+                    cand[lane] = p;
+                }
                 __syncwarp();
                 for (int jj = 0; jj < m; ++jj) {
-                    const Diff d = diff(xi, cand[jj]);
-                    if (valid && d.d2 <= c.r2) {
+                    float d2;
+                    if (kPrecise) {
+                        const float4 xj = cand[jj];
+                        const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+                        d2 = dx * dx + dy * dy + dz * dz;
+                    } else {
+                        d2 = diff(xi, cand[jj]).d2;
+                    }
+                    if (valid && d2 <= c.r2) {
                         if (kFill) out[pos++] = (int64_t)b.id_s[s + jj];
                         ++nn;
                     }
@@ -520,24 +719,37 @@ static int pass_blocks(const LaunchCtx& L) {
 int launch_density(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds) {
     const int threads = 32 * L.warps_per_block;
     const size_t sm = (size_t)L.warps_per_block * sizeof(DensitySmem);
-    static int blocks[5] = {0, 0, 0, 0, 0};
-    if (!blocks[L.warps_per_block]) blocks[L.warps_per_block] = resident_blocks(L, k_density, threads, sm);
-    k_density<<<blocks[L.warps_per_block], threads, sm, L.stream>>>(c, b, ds);
+    static int blocks[2][5] = {{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}};
+    int& nb = blocks[c.precise ? 1 : 0][L.warps_per_block];
+    if (c.precise) {
+        if (!nb) nb = resident_blocks(L, k_density<true>, threads, sm);
+        k_density<true><<<nb, threads, sm, L.stream>>>(c, b, ds);
+    } else {
+        if (!nb) nb = resident_blocks(L, k_density<false>, threads, sm);
+        k_density<false><<<nb, threads, sm, L.stream>>>(c, b, ds);
+    }
     return 1;
+}
+
+template <bool kIntegrate, bool kPrecise>
+static void launch_force_t(const LaunchCtx& L, const StepConst& c, const Buffers& b,
+                           DevState* ds) {
+    const int threads = 32 * L.warps_per_block;
+    const size_t sm = (size_t)L.warps_per_block * sizeof(ForceSmem);
+    static int blocks[5] = {0, 0, 0, 0, 0};
+    int& nb = blocks[L.warps_per_block];
+    if (!nb) nb = resident_blocks(L, k_force<kIntegrate, kPrecise>, threads, sm);
+    k_force<kIntegrate, kPrecise><<<nb, threads, sm, L.stream>>>(c, b, ds);
 }
 
 int launch_force(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds,
                  int integrate) {
-    const int threads = 32 * L.warps_per_block;
-    const size_t sm = (size_t)L.warps_per_block * sizeof(ForceSmem);
-    static int blocks[2][5] = {{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}};
-    int& nb = blocks[integrate ? 1 : 0][L.warps_per_block];
     if (integrate) {
-        if (!nb) nb = resident_blocks(L, k_force<true>, threads, sm);
-        k_force<true><<<nb, threads, sm, L.stream>>>(c, b, ds);
+        if (c.precise) launch_force_t<true, true>(L, c, b, ds);
+        else launch_force_t<true, false>(L, c, b, ds);
     } else {
-        if (!nb) nb = resident_blocks(L, k_force<false>, threads, sm);
-        k_force<false><<<nb, threads, sm, L.stream>>>(c, b, ds);
+        if (c.precise) launch_force_t<false, true>(L, c, b, ds);
+        else launch_force_t<false, false>(L, c, b, ds);
     }
     return 1;
 }
@@ -545,15 +757,23 @@ int launch_force(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevSt
 void launch_pair_counts(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                         DevState* ds, uint32_t* counts_by_id) {
     const size_t sm = (size_t)L.warps_per_block * kTile * sizeof(float4);
-    k_pairs<false><<<pass_blocks(L), 32 * L.warps_per_block, sm, L.stream>>>(
-        c, b, ds, counts_by_id, nullptr, nullptr);
+    if (c.precise)
+        k_pairs<false, true><<<pass_blocks(L), 32 * L.warps_per_block, sm, L.stream>>>(
+            c, b, ds, counts_by_id, nullptr, nullptr);
+    else
+        k_pairs<false, false><<<pass_blocks(L), 32 * L.warps_per_block, sm, L.stream>>>(
+            c, b, ds, counts_by_id, nullptr, nullptr);
 }
 
 void launch_pair_fill(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                       DevState* ds, const uint64_t* offsets_by_id, int64_t* out_idx) {
     const size_t sm = (size_t)L.warps_per_block * kTile * sizeof(float4);
-    k_pairs<true><<<pass_blocks(L), 32 * L.warps_per_block, sm, L.stream>>>(
-        c, b, ds, nullptr, offsets_by_id, out_idx);
+    if (c.precise)
+        k_pairs<true, true><<<pass_blocks(L), 32 * L.warps_per_block, sm, L.stream>>>(
+            c, b, ds, nullptr, offsets_by_id, out_idx);
+    else
+        k_pairs<true, false><<<pass_blocks(L), 32 * L.warps_per_block, sm, L.stream>>>(
+            c, b, ds, nullptr, offsets_by_id, out_idx);
 }
 
 }  // namespace sphx

@@ -23,11 +23,14 @@ ERRORS = {
     -7: "SPHX_ERR_DOMAIN", -8: "SPHX_ERR_OVERFLOW",
 }
 MODE_EXACT = 0
+MODE_PRECISE = 1
+MODE_PRECISE_FP16 = 2
 
 # every symbol include/sphx.h declares
 EXPORTS = (
     "sphx_version", "sphx_strerror", "sphx_create", "sphx_destroy", "sphx_set_stream",
-    "sphx_set_params", "sphx_upload", "sphx_step", "sphx_eval", "sphx_download",
+    "sphx_set_params", "sphx_upload", "sphx_upload_f64", "sphx_step", "sphx_eval",
+    "sphx_download", "sphx_download_f64", "sphx_get_time_f64",
     "sphx_size", "sphx_get_time", "sphx_set_time", "sphx_get_stats", "sphx_reset_stats",
     "sphx_snapshot", "sphx_restore", "sphx_debug_pairs", "sphx_grid_create",
     "sphx_grid_destroy", "sphx_grid_build", "sphx_grid_query", "sphx_grid_info",
@@ -90,6 +93,9 @@ def load_library(path: Path | str = LIB_PATH) -> C.CDLL:
         "sphx_set_stream": ([vp, vp], C.c_int),
         "sphx_set_params": ([vp, C.POINTER(SphxParams)], C.c_int),
         "sphx_upload": ([vp, sz, fp, fp, fp], C.c_int),
+        "sphx_upload_f64": ([vp, sz, fp, fp, fp], C.c_int),
+        "sphx_download_f64": ([vp, fp], C.c_int),
+        "sphx_get_time_f64": ([vp, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
         "sphx_step": ([vp, C.c_float], C.c_int),
         "sphx_eval": ([vp], C.c_int),
         "sphx_download": ([vp, fp, fp, fp, fp, fp], C.c_int),
@@ -189,6 +195,25 @@ class Context:
         self._keep = (pos, vel, mass)
         self._check(self._lib.sphx_upload(self._h, n, _ptr(pos), _ptr(vel), _ptr(mass)),
                     "sphx_upload")
+
+    def upload_f64(self, pos64, vel=None, mass=None):
+        pos64 = np.ascontiguousarray(pos64, np.float64).reshape(-1, 3)
+        n = pos64.shape[0]
+        vel = None if vel is None else _f32(vel).reshape(n, 3)
+        mass = _f32(mass).reshape(n)
+        self._keep = (pos64, vel, mass)
+        self._check(self._lib.sphx_upload_f64(self._h, n, _ptr(pos64), _ptr(vel), _ptr(mass)),
+                    "sphx_upload_f64")
+
+    def positions_f64(self) -> np.ndarray:
+        out = np.empty((self.size(), 3), np.float64)
+        self._check(self._lib.sphx_download_f64(self._h, _ptr(out)), "sphx_download_f64")
+        return out
+
+    def time_f64(self) -> tuple[float, float]:
+        t, dt = C.c_double(), C.c_double()
+        self._check(self._lib.sphx_get_time_f64(self._h, C.byref(t), C.byref(dt)), "sphx_get_time_f64")
+        return t.value, dt.value
 
     def upload_ptr(self, n: int, pos_ptr: int, vel_ptr: int | None, mass_ptr: int):
         """Upload from raw host pointers (e.g. pinned buffers)."""
