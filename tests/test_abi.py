@@ -17,7 +17,7 @@ HEADER = Path(__file__).resolve().parents[1] / "include" / "sphx.h"
 def declared_functions():
     text = HEADER.read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(sphx_[a-z_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(sphx_[a-z0-9_]+)\s*\(", text)))
 
 
 def test_header_declares_the_binding_surface():
