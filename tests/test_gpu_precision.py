@@ -106,6 +106,27 @@ def test_precision_study_errors(study):
     assert half["rho_max"] > cell["rho_max"]
 
 
+def test_precision_study_1M(port):
+    """The configuration at full size: 1,000,000 particles in the periodic unit cube at
+    (1000, 1000, 1000), one evaluation per mode; the error table goes to stdout."""
+    P, V, M, prm, n = periodic_cube(1_000_000, 1.0, 1000.0, seed=2)
+    rho64, _, acc64, _ = port.fields_f64d(P, V, M, prm)
+    scale = np.abs(acc64[:n]).max()
+    rows = {}
+    for name, mode in (("plain_fp32", sphx.MODE_EXACT), ("cell_fp32", sphx.MODE_PRECISE),
+                       ("cell_fp16", sphx.MODE_PRECISE_FP16)):
+        out = evaluate(mode, P, V, M, prm)
+        rel = np.abs(out["rho"][:n].astype(np.float64) - rho64[:n]) / rho64[:n]
+        da = np.abs(out["acc"][:n].astype(np.float64) - acc64[:n]) / scale
+        rows[name] = (rel.max(), rel.mean(), da.max(), da.mean())
+    print("\nprecision study 1M (errors vs FP64): rho max, rho mean, |a| max, |a| mean "
+          "(force errors relative to max |a|)")
+    for k, v in rows.items():
+        print(f"  {k:10s} " + " ".join(f"{x:.3e}" for x in v))
+    assert rows["cell_fp32"][0] <= 1e-5 and rows["cell_fp32"][2] <= 1e-4
+    assert rows["plain_fp32"][0] > 20 * rows["cell_fp32"][0]
+
+
 def test_precise_mode_near_origin_matches_fp64(port):
     w = I.scaled_dam_break(60_000, seed=12)
     ctx = sphx.Context(w.n, mode=sphx.MODE_PRECISE)
@@ -150,12 +171,13 @@ def test_precise_integrator_free_fall_and_walls():
     x = P.copy()
     v = V.astype(np.float64)
     dt = 0.01
+    h = float(np.float32(dt))
     for _ in range(40):
         ctx.step(dt)
-        a = np.array([0.0, -9.81, 0.0])
-        v = v + 0.5 * a * dt
-        x = x + v * dt
-        v = v + 0.5 * a * dt
+        a = np.array([0.0, float(np.float32(-9.81)), 0.0])
+        v = v + 0.5 * a * h
+        x = x + v * h
+        v = v + 0.5 * a * h
         for i in range(3):  # wall at y = 0, restitution 0.8
             if x[i, 1] < 0:
                 x[i, 1] = 0.0
@@ -163,7 +185,8 @@ def test_precise_integrator_free_fall_and_walls():
     got = ctx.positions_f64()
     assert np.abs(got - x).max() < 2e-5
     t, last = ctx.time_f64()
-    assert abs(t - 40 * dt) < 1e-12 and last == pytest.approx(dt)
+    dt32 = float(np.float32(dt))  # step(dt) takes a float; time accumulates it in FP64
+    assert abs(t - 40 * dt32) < 1e-12 and last == dt32
 
 
 def test_precise_cfl_timestep_in_fp64():
