@@ -74,6 +74,8 @@ typedef struct sphx_tuning {
     int64_t max_grid_cells;/* cap on the dense cell grid (cells), >= 125; a larger box of
                               occupied cells is folded per axis; 0 = default */
     int profile;           /* 1 = time each phase with CUDA events (read back lazily) */
+    int graph;             /* 1 = run steps as a captured CUDA graph (recaptured when n,
+                              dt, parameters or scenes change) */
 } sphx_tuning;
 
 /* PerformanceStats (src/sph_engine.h:51-59) plus GPU-side diagnostics. */
@@ -159,6 +161,40 @@ int sphx_upload_f64(sphx_ctx* ctx, size_t n, const double* pos_xyz, const float*
 int sphx_download_f64(sphx_ctx* ctx, double* pos_xyz);
 /* current_time_ and the last dt in FP64 (the FP64 accumulators of the precision modes). */
 int sphx_get_time_f64(sphx_ctx* ctx, double* current_time, double* last_dt);
+
+/* ---- batched scenes --------------------------------------------------------------------
+ * Splits the loaded particles into nscenes independent scenes -- contiguous ranges
+ * [scene_start[s], scene_start[s+1]) of the insertion order, scene_start[0] = 0 and
+ * scene_start[nscenes] = n -- each with its own parameters.  sphx_step then advances every
+ * scene in one launch sequence: each scene exactly as SPHEngine::step would advance it
+ * alone (its own walls, dt/CFL from its own particles and its own first particle's
+ * acceleration, its own time), bit for bit; no particle meets another scene's.  The cell
+ * boxes of all scenes together must fit max_grid_cells (else SPHX_ERR_DOMAIN).  Exact mode
+ * only.  sphx_upload resets to a single scene; nscenes = 0 does too.  No counterpart in
+ * the reference, which runs one scene per SPHEngine. */
+int sphx_set_scenes(sphx_ctx* ctx, uint32_t nscenes, const uint64_t* scene_start,
+                    const sphx_params* params);
+
+typedef struct sphx_scene_stats {
+    uint64_t start, count;
+    float current_time;
+    float last_dt;
+    uint32_t grid_cells;
+    uint32_t pad;
+    double sum_mass;
+    double momentum[3];
+    double kinetic_energy;
+    double potential_energy;
+} sphx_scene_stats;
+/* Time, dt and FP64 conservation sums of one scene after the last step (synchronises). */
+int sphx_get_scene_stats(sphx_ctx* ctx, uint32_t scene, sphx_scene_stats* out);
+
+/* Picks the neighbour passes' launch shape for the loaded workload: times two steps of
+ * dt for each candidate (warps per CTA x resident CTAs per SM), restores the particles,
+ * times and scene records after every trial, and keeps the fastest in the context.
+ * Returns the choice and its time per step.  Synchronises. */
+int sphx_autotune(sphx_ctx* ctx, float dt, int* warps_per_block, int* blocks_per_sm,
+                  float* best_ms);
 
 /* Number of particles currently loaded. */
 int sphx_size(sphx_ctx* ctx, size_t* n);

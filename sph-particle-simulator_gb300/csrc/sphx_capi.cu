@@ -35,6 +35,19 @@ struct sphx_ctx {
     double t_total = 0, t_nb = 0, t_den = 0, t_force = 0;
     // per-phase timing: events recorded into a ring, read back only when a slot is reused
     // or the stats are requested, so profiling adds no per-step host sync
+    // batched scenes
+    uint32_t nscenes = 0;
+    uint32_t scene_cap = 0;
+    std::vector<sphx_params> scene_params;
+    std::vector<uint64_t> scene_start;
+    // CUDA graph of the step (tuning.graph): captured after one warm-up step, replayed
+    // while n, dt, parameters and scenes stay the same
+    cudaGraphExec_t graph_exec = nullptr;
+    bool graph_warm = false;
+    uint64_t graph_version = ~0ull;
+    float graph_dt = 0.0f;
+    int graph_launches = 0;
+    uint64_t version = 0;  // bumped by every change the graph depends on
     static constexpr int kProfRing = 64;
     struct ProfSlot {
         cudaEvent_t ev[5];
@@ -82,10 +95,13 @@ float host_cubic_w(float sigma, float q) {
     return 0.0f;
 }
 
-void fill_step_const(sphx_ctx* c) {
-    const sphx_params& p = c->params;
-    StepConst& s = c->sc;
-    s.n = (int)c->n;
+void fill_step_const_from(sphx_ctx* c, const sphx_params& p, size_t n, StepConst& s);
+
+void fill_step_const(sphx_ctx* c) { fill_step_const_from(c, c->params, c->n, c->sc); }
+
+void fill_step_const_from(sphx_ctx* c, const sphx_params& p, size_t n, StepConst& s) {
+    s.max_cells = c->sc.max_cells;
+    s.n = (int)n;
     // SpatialHash::set_cell_size(neighbor_search_radius): inv = 1.0f / cell
     s.inv_cell = 1.0f / p.neighbor_search_radius;
     s.r2 = p.neighbor_search_radius * p.neighbor_search_radius;
@@ -136,12 +152,14 @@ void free_all(sphx_ctx* c) {
     void* ptrs[] = {b.pos4, b.vel4,   b.pos4_s, b.vel4_s,     b.aux4_s,    b.acc4_s,
                     b.key[0], b.key[1], b.val[0], b.val[1],   b.key_s,     b.id_s,
                     b.off,  b.tile_start, b.hist, b.scan_part, b.diag_part, c->ds,
-                    c->stage, c->snap_pos, c->snap_vel, c->snap_cell, b.cell4, b.cell4_s};
+                    c->stage, c->snap_pos, c->snap_vel, c->snap_cell, b.cell4, b.cell4_s,
+                    b.scene_of, b.scene_s, b.scenes};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto& slot : c->prof)
         for (auto& e : slot.ev)
             if (e) cudaEventDestroy(e);
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
 }
 
@@ -191,21 +209,73 @@ int run_phases(sphx_ctx* c, float dt, bool integrate) {
         if (rc) return rc;
         SPHX_CUDA(cudaEventRecord(slot->ev[0], c->stream));
     }
-    int k = launch_begin_step(c->L, c->ds, 1);
-    if (integrate) k += launch_cfl(c->L, c->sc, c->b, c->ds, dt);
-    k += launch_build_grid(c->L, c->sc, c->b, c->ds);
+    const bool batch = c->b.nscenes > 0;
+    int k = 0;
+    if (batch) {
+        k += launch_batch_begin(c->L, c->b, c->ds);
+        if (integrate) k += launch_batch_cfl(c->L, c->b, c->ds, (int)c->n, dt);
+        k += launch_batch_grid(c->L, c->b, c->ds, (int)c->n, c->sc.max_cells);
+    } else {
+        k += launch_begin_step(c->L, c->ds, 1);
+        if (integrate) k += launch_cfl(c->L, c->sc, c->b, c->ds, dt);
+        k += launch_build_grid(c->L, c->sc, c->b, c->ds);
+    }
     if (slot) SPHX_CUDA(cudaEventRecord(slot->ev[1], c->stream));
     k += launch_density(c->L, c->sc, c->b, c->ds);
     if (slot) SPHX_CUDA(cudaEventRecord(slot->ev[2], c->stream));
     k += launch_force(c->L, c->sc, c->b, c->ds, integrate ? 1 : 0);
     if (slot) SPHX_CUDA(cudaEventRecord(slot->ev[3], c->stream));
-    if (integrate) k += launch_diag(c->L, c->sc, c->b, c->ds);
+    if (integrate) k += batch ? launch_batch_diag(c->L, c->b, c->ds) : launch_diag(c->L, c->sc, c->b, c->ds);
     if (slot) {
         SPHX_CUDA(cudaEventRecord(slot->ev[4], c->stream));
         slot->pending = true;
     }
     SPHX_CUDA(cudaGetLastError());
     c->launches += (uint64_t)k;
+    c->graph_launches = k;
+    c->have_fields = true;
+    return SPHX_OK;
+}
+
+// One step through a CUDA graph: the first step of a configuration runs eagerly (it warms
+// up the per-kernel launch shapes), the next one is captured, later ones replay it.
+int run_step_graph(sphx_ctx* c, float dt) {
+    const bool same = c->graph_exec && c->graph_version == c->version && c->graph_dt == dt;
+    if (!same) {
+        if (c->graph_exec) {
+            cudaGraphExecDestroy(c->graph_exec);
+            c->graph_exec = nullptr;
+        }
+        if (!c->graph_warm || c->graph_version != c->version) {
+            c->graph_warm = true;
+            c->graph_version = c->version;
+            c->graph_dt = dt;
+            return run_phases(c, dt, true);
+        }
+        const int saved = c->tuning.profile;
+        c->tuning.profile = 0;  // no host-side event reads inside a capture
+        SPHX_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = run_phases(c, dt, true);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        c->tuning.profile = saved;
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return cuda_fail(e);
+        const cudaError_t ei = cudaGraphInstantiate(&c->graph_exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) {
+            c->graph_exec = nullptr;
+            return cuda_fail(ei);
+        }
+        c->graph_version = c->version;
+        c->graph_dt = dt;
+        c->launches -= (uint64_t)c->graph_launches;  // captured, not launched
+    }
+    SPHX_CUDA(cudaGraphLaunch(c->graph_exec, c->stream));
+    c->launches += (uint64_t)c->graph_launches;
     c->have_fields = true;
     return SPHX_OK;
 }
@@ -347,6 +417,7 @@ int sphx_set_params(sphx_ctx* c, const sphx_params* p) {
     }
     c->params = *p;
     c->have_params = true;
+    c->version++;
     return SPHX_OK;
 }
 
@@ -375,6 +446,9 @@ int sphx_upload(sphx_ctx* c, size_t n, const float* pos, const float* vel, const
     }
     c->n = n;
     c->have_fields = false;
+    c->b.nscenes = 0;  // a new particle set: scenes must be set again
+    c->nscenes = 0;
+    c->version++;
     return SPHX_OK;
 }
 
@@ -411,6 +485,9 @@ int sphx_upload_f64(sphx_ctx* c, size_t n, const double* pos, const float* vel,
     }
     c->n = n;
     c->have_fields = false;
+    c->b.nscenes = 0;  // a new particle set: scenes must be set again
+    c->nscenes = 0;
+    c->version++;
     return SPHX_OK;
 }
 
@@ -425,10 +502,172 @@ int sphx_step(sphx_ctx* c, float dt) {
     if (rc) return rc;
     if (c->n == 0) return SPHX_OK;  // SPHEngine::step returns when empty (cpp:94)
     if (!c->have_params) return SPHX_ERR_NOT_READY;
-    rc = run_phases(c, dt, true);
+    rc = c->tuning.graph ? run_step_graph(c, dt) : run_phases(c, dt, true);
     if (rc) return rc;
     c->steps++;
     c->queries += c->n;
+    return SPHX_OK;
+}
+
+int sphx_set_scenes(sphx_ctx* c, uint32_t nscenes, const uint64_t* scene_start,
+                    const sphx_params* params) {
+    int rc = enter(c);
+    if (rc) return rc;
+    if (nscenes == 0) {
+        c->b.nscenes = 0;
+        c->nscenes = 0;
+        c->version++;
+        return SPHX_OK;
+    }
+    if (!scene_start || !params) return SPHX_ERR_INVALID_ARG;
+    if (c->tuning.mode != SPHX_MODE_EXACT) return SPHX_ERR_INVALID_ARG;
+    if (scene_start[0] != 0 || scene_start[nscenes] != c->n) return SPHX_ERR_INVALID_ARG;
+    for (uint32_t s = 0; s < nscenes; ++s) {
+        if (scene_start[s + 1] < scene_start[s]) return SPHX_ERR_INVALID_ARG;
+        const float r = params[s].neighbor_search_radius;
+        if (!(r > 0.0f) || !std::isfinite(r) || !std::isfinite(1.0f / r)) return SPHX_ERR_INVALID_ARG;
+    }
+    Buffers& b = c->b;
+    if (!b.scene_of) {
+        if ((rc = dmalloc(&b.scene_of, c->capacity)) || (rc = dmalloc(&b.scene_s, c->capacity)))
+            return rc;
+    }
+    if (nscenes > c->scene_cap) {
+        if (b.scenes) cudaFree(b.scenes);
+        b.scenes = nullptr;
+        if ((rc = dmalloc(&b.scenes, nscenes))) return rc;
+        c->scene_cap = nscenes;
+    }
+    std::vector<SceneInfo> info(nscenes);
+    std::vector<uint32_t> owner(c->n);
+    for (uint32_t s = 0; s < nscenes; ++s) {
+        SceneInfo& si = info[s];
+        std::memset(&si, 0, sizeof(si));
+        si.start = (uint32_t)scene_start[s];
+        si.count = (uint32_t)(scene_start[s + 1] - scene_start[s]);
+        fill_step_const_from(c, params[s], si.count, si.c);
+        for (uint64_t i = scene_start[s]; i < scene_start[s + 1]; ++i) owner[i] = s;
+    }
+    SPHX_CUDA(cudaStreamSynchronize(c->stream));
+    SPHX_CUDA(cudaMemcpy(b.scenes, info.data(), nscenes * sizeof(SceneInfo), cudaMemcpyHostToDevice));
+    if (c->n) SPHX_CUDA(cudaMemcpy(b.scene_of, owner.data(), c->n * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    c->scene_params.assign(params, params + nscenes);
+    c->scene_start.assign(scene_start, scene_start + nscenes + 1);
+    c->nscenes = nscenes;
+    b.nscenes = (int)nscenes;
+    if (!c->have_params) {  // the context-wide parameters default to the first scene's
+        c->params = params[0];
+        c->have_params = true;
+    }
+    c->have_fields = false;
+    c->version++;
+    return SPHX_OK;
+}
+
+int sphx_autotune(sphx_ctx* c, float dt, int* warps_per_block, int* blocks_per_sm,
+                  float* best_ms) {
+    int rc = enter(c);
+    if (rc) return rc;
+    if (!c->have_params) return SPHX_ERR_NOT_READY;
+    if (c->n == 0) return SPHX_OK;
+    // save everything a step changes: device state words, scene records, particles
+    SPHX_CUDA(cudaStreamSynchronize(c->stream));
+    DevState ds_save;
+    SPHX_CUDA(cudaMemcpy(&ds_save, c->ds, sizeof(DevState), cudaMemcpyDeviceToHost));
+    std::vector<SceneInfo> sc_save(c->nscenes);
+    if (c->nscenes)
+        SPHX_CUDA(cudaMemcpy(sc_save.data(), c->b.scenes, c->nscenes * sizeof(SceneInfo), cudaMemcpyDeviceToHost));
+    const bool had_snap = c->snap_pos != nullptr;
+    std::vector<float4> keep_pos, keep_vel;
+    std::vector<int4> keep_cell;
+    if (had_snap) {  // the caller's snapshot must survive: keep it on the host meanwhile
+        keep_pos.resize(c->n);
+        keep_vel.resize(c->n);
+        SPHX_CUDA(cudaMemcpy(keep_pos.data(), c->snap_pos, c->n * sizeof(float4), cudaMemcpyDeviceToHost));
+        SPHX_CUDA(cudaMemcpy(keep_vel.data(), c->snap_vel, c->n * sizeof(float4), cudaMemcpyDeviceToHost));
+        if (c->snap_cell) {
+            keep_cell.resize(c->n);
+            SPHX_CUDA(cudaMemcpy(keep_cell.data(), c->snap_cell, c->n * sizeof(int4), cudaMemcpyDeviceToHost));
+        }
+    }
+    if ((rc = sphx_snapshot(c))) return rc;
+    const int saved_profile = c->tuning.profile;
+    const uint64_t saved_launches = c->launches;
+    c->tuning.profile = 0;
+    cudaEvent_t e0, e1;
+    SPHX_CUDA(cudaEventCreate(&e0));
+    SPHX_CUDA(cudaEventCreate(&e1));
+    const int cand[][2] = {{4, 0}, {2, 0}, {4, 4}, {4, 2}, {2, 4}, {1, 0}};
+    float best = 0.0f;
+    int bw = c->L.warps_per_block, bb = c->L.blocks_per_sm;
+    auto reset = [&]() -> int {
+        SPHX_CUDA(cudaMemcpyAsync(c->ds, &ds_save, sizeof(DevState), cudaMemcpyHostToDevice, c->stream));
+        if (c->nscenes)
+            SPHX_CUDA(cudaMemcpyAsync(c->b.scenes, sc_save.data(), c->nscenes * sizeof(SceneInfo), cudaMemcpyHostToDevice, c->stream));
+        SPHX_CUDA(cudaStreamSynchronize(c->stream));
+        return sphx_restore(c);
+    };
+    for (const auto& cd : cand) {
+        c->L.warps_per_block = cd[0];
+        c->L.blocks_per_sm = cd[1];
+        if ((rc = reset()) || (rc = run_phases(c, dt, true))) break;  // warm-up
+        if ((rc = reset())) break;
+        SPHX_CUDA(cudaEventRecord(e0, c->stream));
+        if ((rc = run_phases(c, dt, true))) break;
+        if ((rc = reset())) break;  // identical work for the second timed step
+        if ((rc = run_phases(c, dt, true))) break;
+        SPHX_CUDA(cudaEventRecord(e1, c->stream));
+        SPHX_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        SPHX_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (best == 0.0f || ms < best) {
+            best = ms;
+            bw = cd[0];
+            bb = cd[1];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->L.warps_per_block = bw;
+    c->L.blocks_per_sm = bb;
+    c->tuning.warps_per_block = bw;
+    c->tuning.blocks_per_sm = bb;
+    c->tuning.profile = saved_profile;
+    c->launches = saved_launches;
+    int rc2 = reset();
+    if (had_snap) {  // put the caller's snapshot back
+        SPHX_CUDA(cudaMemcpy(c->snap_pos, keep_pos.data(), c->n * sizeof(float4), cudaMemcpyHostToDevice));
+        SPHX_CUDA(cudaMemcpy(c->snap_vel, keep_vel.data(), c->n * sizeof(float4), cudaMemcpyHostToDevice));
+        if (c->snap_cell)
+            SPHX_CUDA(cudaMemcpy(c->snap_cell, keep_cell.data(), c->n * sizeof(int4), cudaMemcpyHostToDevice));
+    }
+    c->have_fields = false;
+    c->version++;
+    if (warps_per_block) *warps_per_block = bw;
+    if (blocks_per_sm) *blocks_per_sm = bb;
+    if (best_ms) *best_ms = best / 2.0f;
+    return rc ? rc : rc2;
+}
+
+int sphx_get_scene_stats(sphx_ctx* c, uint32_t scene, sphx_scene_stats* out) {
+    int rc = enter(c);
+    if (rc) return rc;
+    if (!out || scene >= c->nscenes) return SPHX_ERR_INVALID_ARG;
+    SPHX_CUDA(cudaStreamSynchronize(c->stream));
+    SceneInfo si;
+    SPHX_CUDA(cudaMemcpy(&si, c->b.scenes + scene, sizeof(SceneInfo), cudaMemcpyDeviceToHost));
+    std::memset(out, 0, sizeof(*out));
+    out->start = si.start;
+    out->count = si.count;
+    out->current_time = si.time;
+    out->last_dt = si.dt;
+    out->grid_cells = si.ncells;
+    out->sum_mass = si.sums[0];
+    out->momentum[0] = si.sums[1];
+    out->momentum[1] = si.sums[2];
+    out->momentum[2] = si.sums[3];
+    out->kinetic_energy = si.sums[4];
+    out->potential_energy = si.sums[5];
     return SPHX_OK;
 }
 

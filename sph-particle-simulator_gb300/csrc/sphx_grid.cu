@@ -292,6 +292,7 @@ __global__ void k_reorder(const Buffers b, int n, DevState* ds) {
         b.pos4_s[k] = b.pos4[id];
         b.vel4_s[k] = b.vel4[id];
         if (b.cell4) b.cell4_s[k] = b.cell4[id];
+        if (b.scene_s) b.scene_s[k] = b.scene_of[id];
     }
 }
 
@@ -317,10 +318,16 @@ int launch_build_grid(const LaunchCtx& L, const StepConst& c, const Buffers& b,
     k_grid_setup<<<1, 32, 0, L.stream>>>(n, c.max_cells, ds);
     if (c.precise) k_keys_cells<<<gb, 256, 0, L.stream>>>(b.cell4, n, ds, b.key[0]);
     else k_keys<<<gb, 256, 0, L.stream>>>(b.pos4, n, c.inv_cell, ds, b.key[0]);
+    return 3 + launch_grid_sort(L, b, ds, n);
+}
+
+// Shared tail of the grid build: stable sort of the keys, gather into cell-sorted order,
+// cell offsets, tile list.
+int launch_grid_sort(const LaunchCtx& L, const Buffers& b, DevState* ds, int n) {
     const int r = launch_radix_sort(L, b, ds, n);
     k_reorder<<<grid_blocks(L, n, 256, 8), 256, 0, L.stream>>>(b, n, ds);
     k_offsets<<<grid_blocks(L, n + 1, 256, 8), 256, 0, L.stream>>>(b.key_s, n, ds, b.off);
-    return 5 + r + launch_tile_scan(L, b, ds, n);
+    return 2 + r + launch_tile_scan(L, b, ds, n);
 }
 
 // ---- FP64 diagnostics of the state after a step -----------------------------------------

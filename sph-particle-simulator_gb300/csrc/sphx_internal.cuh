@@ -66,6 +66,29 @@ struct DevState {
     unsigned long long vmax64;  // precision mode: max |v| (FP64 bits)
 };
 
+// Batched mode: one record per scene (device memory).  Scenes are contiguous ranges of
+// the insertion order; each owns a dense block of grid cells starting at `base`.
+struct SceneInfo {
+    StepConst c;                // the scene's parameters and constants (c.n = count)
+    uint32_t start, count;      // particle range in insertion order
+    int cmin[3], cmax[3];       // box of occupied cells
+    int dim[3];                 // grid extent of the scene
+    uint32_t base, ncells;      // first grid cell, number of cells
+    uint32_t nonfinite;
+    uint32_t vmax_bits;
+    float dt, time;             // the scene's dt of the current step and current_time_
+    float a0[4];                // acceleration of the scene's first particle
+    double sums[kDiagSums];     // FP64 diagnostics of the scene after the last step
+};
+
+// Grid geometry of one tile: the whole grid (single scene) or the tile's scene block.
+struct Geom {
+    int dim[3];
+    int wrap[3];
+    uint32_t base;      // first cell of the block
+    uint32_t sentinel;  // key of the non-finite group (total number of cells)
+};
+
 struct Buffers {
     float4* pos4;     // insertion order: x, y, z, mass
     float4* vel4;     // insertion order: vx, vy, vz, 0
@@ -84,6 +107,10 @@ struct Buffers {
     uint32_t* hist;   // radix histograms / offsets
     uint32_t* scan_part;
     double* diag_part;
+    uint32_t* scene_of;  // batched mode: scene of each particle (insertion order)
+    uint32_t* scene_s;   // batched mode: scene of each particle (cell-sorted)
+    SceneInfo* scenes;   // batched mode: per-scene records
+    int nscenes;         // 0: single scene
     int radix_blocks;
     int scan_part_cap;
     int diag_blocks;
@@ -183,6 +210,7 @@ int launch_cfl(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevStat
                 float host_dt);
 int launch_build_grid(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                        DevState* ds);
+int launch_grid_sort(const LaunchCtx& L, const Buffers& b, DevState* ds, int n);
 int launch_density(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds);
 int launch_force(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds,
                   int integrate);
@@ -191,6 +219,13 @@ void launch_pair_counts(const LaunchCtx& L, const StepConst& c, const Buffers& b
                         DevState* ds, uint32_t* counts_by_id);
 void launch_pair_fill(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                       DevState* ds, const uint64_t* offsets_by_id, int64_t* out_idx);
+
+// batched mode (sphx_batch.cu)
+int launch_batch_begin(const LaunchCtx& L, const Buffers& b, DevState* ds);
+int launch_batch_cfl(const LaunchCtx& L, const Buffers& b, DevState* ds, int n, float host_dt);
+int launch_batch_grid(const LaunchCtx& L, const Buffers& b, DevState* ds, int n,
+                      uint32_t max_cells);
+int launch_batch_diag(const LaunchCtx& L, const Buffers& b, DevState* ds);
 
 // radix sort + scan (sphx_sort.cu)
 int launch_radix_sort(const LaunchCtx& L, const Buffers& b, DevState* ds, int n);

@@ -30,24 +30,48 @@ struct Tile {
     int lo[3], hi[3];
 };
 
-// Sets up tile t for this warp; returns the lane's particle (valid lanes only).
-__device__ __forceinline__ void tile_setup(const StepConst& c, const Buffers& b,
-                                           const DevState* ds, uint32_t t, int lane, Tile& T,
-                                           float4& xi, bool& valid) {
-    const uint32_t k0 = b.tile_start[t];
+// Geometry of the whole grid (single scene).
+__device__ __forceinline__ Geom grid_geom(const DevState* ds) {
+    Geom g;
+    for (int a = 0; a < 3; ++a) {
+        g.dim[a] = ds->dim[a];
+        g.wrap[a] = ds->wrap[a];
+    }
+    g.base = 0;
+    g.sentinel = ds->ncells;
+    return g;
+}
+
+// Geometry of one scene's block of cells (batched mode; scene grids are never folded).
+__device__ __forceinline__ Geom scene_geom(const SceneInfo& sc, const DevState* ds) {
+    Geom g;
+    for (int a = 0; a < 3; ++a) {
+        g.dim[a] = sc.dim[a];
+        g.wrap[a] = 0;
+    }
+    g.base = sc.base;
+    g.sentinel = ds->ncells;
+    return g;
+}
+
+// Sets up the tile starting at sorted position k0; returns the lane's particle (valid
+// lanes only).
+__device__ __forceinline__ void tile_setup(const StepConst& c, const Buffers& b, const Geom& g,
+                                           uint32_t k0, int lane, Tile& T, float4& xi,
+                                           bool& valid) {
     const uint32_t key = b.key_s[k0];
-    const uint32_t nc = ds->ncells;
     const uint32_t end = b.off[key + 1];
     T.k0 = (int)k0;
     T.cnt = (int)min(end - k0, (uint32_t)kTile);
     valid = lane < T.cnt;
     xi = valid ? b.pos4_s[k0 + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
-    T.cells = key < nc;
+    T.cells = key < g.sentinel;
     if (!T.cells) return;
-    const uint32_t dz = ds->dim[2], dy = ds->dim[1];
-    T.cz = (int)(key % dz);
-    T.cy = (int)((key / dz) % dy);
-    T.cx = (int)(key / (dz * dy));
+    const uint32_t local = key - g.base;
+    const uint32_t dz = g.dim[2], dy = g.dim[1];
+    T.cz = (int)(local % dz);
+    T.cy = (int)((local / dz) % dy);
+    T.cx = (int)(local / (dz * dy));
     const float x[3] = {xi.x, xi.y, xi.z};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -73,12 +97,11 @@ __device__ __forceinline__ float4 frame_pos(const int4& cell, const int4& frame,
 }
 
 __device__ __forceinline__ void tile_setup_cells(const StepConst& c, const Buffers& b,
-                                                 const DevState* ds, uint32_t t, int lane,
+                                                 const Geom& g, uint32_t k0, int lane,
                                                  Tile& T, float4& xi, bool& valid,
                                                  int4& frame) {
-    const uint32_t k0 = b.tile_start[t];
     const uint32_t key = b.key_s[k0];
-    const uint32_t nc = ds->ncells;
+    const uint32_t nc = g.sentinel;
     const uint32_t end = b.off[key + 1];
     T.k0 = (int)k0;
     T.cnt = (int)min(end - k0, (uint32_t)kTile);
@@ -92,10 +115,11 @@ __device__ __forceinline__ void tile_setup_cells(const StepConst& c, const Buffe
         xi = o;
         return;
     }
-    const uint32_t dz = ds->dim[2], dy = ds->dim[1];
-    T.cz = (int)(key % dz);
-    T.cy = (int)((key / dz) % dy);
-    T.cx = (int)(key / (dz * dy));
+    const uint32_t local = key - g.base;
+    const uint32_t dz = g.dim[2], dy = g.dim[1];
+    T.cz = (int)(local % dz);
+    T.cy = (int)((local / dz) % dy);
+    T.cx = (int)(local / (dz * dy));
     const float off[3] = {o.x, o.y, o.z};
     const float eps = c.cs * 2.44140625e-4f;  // 2^-12 cells
 #pragma unroll
@@ -111,11 +135,11 @@ __device__ __forceinline__ void tile_setup_cells(const StepConst& c, const Buffe
 // folded axis the neighbour index wraps; a row that wraps on z is two segments, visited
 // in dz order.
 template <class F>
-__device__ __forceinline__ void for_each_row(const Buffers& b, const DevState* ds,
-                                             const Tile& T, F&& f) {
+__device__ __forceinline__ void for_each_row(const Buffers& b, const Geom& g, const Tile& T,
+                                             F&& f) {
     if (!T.cells) return;
-    const int d0 = ds->dim[0], d1 = ds->dim[1], d2 = ds->dim[2];
-    const bool w0 = ds->wrap[0], w1 = ds->wrap[1], w2 = ds->wrap[2];
+    const int d0 = g.dim[0], d1 = g.dim[1], d2 = g.dim[2];
+    const bool w0 = g.wrap[0], w1 = g.wrap[1], w2 = g.wrap[2];
     // z range of every row: [z0, z1] plus, when z wraps past the end, [0, z2]
     int z0 = T.cz + T.lo[2], z1 = T.cz + T.hi[2], z2 = -1;
     int zp = -1, zq = -2;  // a wrapped piece at the front (dz < 0 past 0)
@@ -141,7 +165,7 @@ __device__ __forceinline__ void for_each_row(const Buffers& b, const DevState* d
             int Y = T.cy + dy;
             if (w1) Y = (Y + d1) % d1;
             else if (Y < 0 || Y >= d1) continue;
-            const uint32_t rb = ((uint32_t)X * (uint32_t)d1 + (uint32_t)Y) * (uint32_t)d2;
+            const uint32_t rb = g.base + ((uint32_t)X * (uint32_t)d1 + (uint32_t)Y) * (uint32_t)d2;
             if (zp <= zq) {
                 const uint32_t a = b.off[rb + zp], e = b.off[rb + zq + 1];
                 if (a < e) f((int)a, (int)e);
@@ -286,24 +310,28 @@ struct DensitySmem {
     float tbuf[kDensityBatch];
 };
 
-template <bool kPrecise>
-__global__ void __launch_bounds__(128, 8) k_density(const StepConst c, const Buffers b,
+template <bool kPrecise, bool kBatch>
+__global__ void __launch_bounds__(128, 8) k_density(const StepConst cp, const Buffers b,
                                                  DevState* ds) {
     if (ds->status) return;
     extern __shared__ __align__(16) unsigned char smem_raw_d[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     DensitySmem* S = reinterpret_cast<DensitySmem*>(smem_raw_d) + warp;
     const uint32_t ntiles = ds->n_tiles;
-    const float r2m = c.r2 * 1.0001f;
     const float inf = __int_as_float(0x7f800000);
     uint32_t my_max = 0;
     for (uint32_t t = next_tile(&ds->work[0], lane); t < ntiles; t = next_tile(&ds->work[0], lane)) {
+        const uint32_t k0 = b.tile_start[t];
+        const int scene = kBatch ? (int)b.scene_s[k0] : 0;
+        const StepConst& c = kBatch ? b.scenes[scene].c : cp;
+        const Geom g = kBatch ? scene_geom(b.scenes[scene], ds) : grid_geom(ds);
+        const float r2m = c.r2 * 1.0001f;
         Tile T;
         float4 xi;
         bool valid;
         int4 frame = make_int4(0, 0, 0, 0);
-        if (kPrecise) tile_setup_cells(c, b, ds, t, lane, T, xi, valid, frame);
-        else tile_setup(c, b, ds, t, lane, T, xi, valid);
+        if (kPrecise) tile_setup_cells(c, b, g, k0, lane, T, xi, valid, frame);
+        else tile_setup(c, b, g, k0, lane, T, xi, valid);
         const int i = T.k0 + lane;
         const TileBox B = tile_box(xi, valid);
         S->tpos[lane] = xi;
@@ -311,7 +339,7 @@ __global__ void __launch_bounds__(128, 8) k_density(const StepConst c, const Buf
         KSum rk;
         rk.s = rho;
         uint32_t nn = 0;
-        for_each_row(b, ds, T, [&](int a, int e) {
+        for_each_row(b, g, T, [&](int a, int e) {
             for (int s = a; s < e; s += kTile) {
                 const int m = min(kTile, e - s);
                 __syncwarp();
@@ -488,24 +516,28 @@ __device__ __forceinline__ void integrate_cells(const StepConst& c, float dt, co
     }
 }
 
-template <bool kIntegrate, bool kPrecise>
-__global__ void __launch_bounds__(128, 6) k_force(const StepConst c, const Buffers b,
+template <bool kIntegrate, bool kPrecise, bool kBatch>
+__global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buffers b,
                                                DevState* ds) {
     if (ds->status) return;
     extern __shared__ __align__(16) unsigned char smem_raw_f[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     ForceSmem* S = reinterpret_cast<ForceSmem*>(smem_raw_f) + warp;
     const uint32_t ntiles = ds->n_tiles;
-    const float dt = ds->dt;
-    const float r2m = c.r2 * 1.0001f;
     const float inf = __int_as_float(0x7f800000);
     for (uint32_t t = next_tile(&ds->work[1], lane); t < ntiles; t = next_tile(&ds->work[1], lane)) {
+        const uint32_t k0 = b.tile_start[t];
+        const int scene = kBatch ? (int)b.scene_s[k0] : 0;
+        const StepConst& c = kBatch ? b.scenes[scene].c : cp;
+        const Geom g = kBatch ? scene_geom(b.scenes[scene], ds) : grid_geom(ds);
+        const float dt = kBatch ? b.scenes[scene].dt : ds->dt;
+        const float r2m = c.r2 * 1.0001f;
         Tile T;
         float4 xi;
         bool valid;
         int4 frame = make_int4(0, 0, 0, 0);
-        if (kPrecise) tile_setup_cells(c, b, ds, t, lane, T, xi, valid, frame);
-        else tile_setup(c, b, ds, t, lane, T, xi, valid);
+        if (kPrecise) tile_setup_cells(c, b, g, k0, lane, T, xi, valid, frame);
+        else tile_setup(c, b, g, k0, lane, T, xi, valid);
         const int i = T.k0 + lane;
         const float4 vi = valid ? b.vel4_s[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float Pi = valid ? b.aux4_s[i].y : 0.0f;
@@ -516,7 +548,7 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst c, const Buffe
         float fpx = 0.0f, fpy = 0.0f, fpz = 0.0f;
         float fvx = 0.0f, fvy = 0.0f, fvz = 0.0f;
         KSum Fx, Fy, Fz;  // precision mode: one compensated sum per component
-        for_each_row(b, ds, T, [&](int a, int e) {
+        for_each_row(b, g, T, [&](int a, int e) {
             for (int s = a; s < e; s += kTile) {
                 const int m = min(kTile, e - s);
                 __syncwarp();
@@ -637,7 +669,13 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst c, const Buffe
         }
         b.pos4[id] = make_float4(x[0], x[1], x[2], mi);
         b.vel4[id] = make_float4(v[0], v[1], v[2], 0.0f);
-        if (id == 0) {
+        if (kBatch) {
+            if (id == b.scenes[scene].start) {  // accelerations_[0] of the scene
+                b.scenes[scene].a0[0] = ax;
+                b.scenes[scene].a0[1] = ay;
+                b.scenes[scene].a0[2] = az;
+            }
+        } else if (id == 0) {
             ds->a0[0] = ax;
             ds->a0[1] = ay;
             ds->a0[2] = az;
@@ -659,17 +697,19 @@ __global__ void __launch_bounds__(128) k_pairs(const StepConst c, const Buffers 
     const int nwarps = gridDim.x * (blockDim.x >> 5);
     const uint32_t ntiles = ds->n_tiles;
     for (uint32_t t = blockIdx.x * (blockDim.x >> 5) + warp; t < ntiles; t += nwarps) {
+        const uint32_t k0 = b.tile_start[t];
+        const Geom g = grid_geom(ds);
         Tile T;
         float4 xi;
         bool valid;
         int4 frame = make_int4(0, 0, 0, 0);
-        if (kPrecise) tile_setup_cells(c, b, ds, t, lane, T, xi, valid, frame);
-        else tile_setup(c, b, ds, t, lane, T, xi, valid);
+        if (kPrecise) tile_setup_cells(c, b, g, k0, lane, T, xi, valid, frame);
+        else tile_setup(c, b, g, k0, lane, T, xi, valid);
         const int i = T.k0 + lane;
         const uint32_t id = valid ? b.id_s[i] : 0u;
         uint64_t pos = (kFill && valid) ? off_by_id[id] : 0ull;
         uint32_t nn = 0;
-        for_each_row(b, ds, T, [&](int a, int e) {
+        for_each_row(b, g, T, [&](int a, int e) {
             for (int s = a; s < e; s += kTile) {
                 const int m = min(kTile, e - s);
                 __syncwarp();
@@ -716,40 +756,46 @@ static int pass_blocks(const LaunchCtx& L) {
     return L.num_sms * bps;
 }
 
-int launch_density(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds) {
+template <bool kPrecise, bool kBatch>
+static void launch_density_t(const LaunchCtx& L, const StepConst& c, const Buffers& b,
+                             DevState* ds) {
     const int threads = 32 * L.warps_per_block;
     const size_t sm = (size_t)L.warps_per_block * sizeof(DensitySmem);
-    static int blocks[2][5] = {{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}};
-    int& nb = blocks[c.precise ? 1 : 0][L.warps_per_block];
-    if (c.precise) {
-        if (!nb) nb = resident_blocks(L, k_density<true>, threads, sm);
-        k_density<true><<<nb, threads, sm, L.stream>>>(c, b, ds);
-    } else {
-        if (!nb) nb = resident_blocks(L, k_density<false>, threads, sm);
-        k_density<false><<<nb, threads, sm, L.stream>>>(c, b, ds);
-    }
+    static int blocks[5][8] = {};
+    int& nb = blocks[L.warps_per_block][L.blocks_per_sm & 7];
+    if (!nb) nb = resident_blocks(L, k_density<kPrecise, kBatch>, threads, sm);
+    k_density<kPrecise, kBatch><<<nb, threads, sm, L.stream>>>(c, b, ds);
+}
+
+int launch_density(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds) {
+    if (b.nscenes > 0) launch_density_t<false, true>(L, c, b, ds);
+    else if (c.precise) launch_density_t<true, false>(L, c, b, ds);
+    else launch_density_t<false, false>(L, c, b, ds);
     return 1;
 }
 
-template <bool kIntegrate, bool kPrecise>
+template <bool kIntegrate, bool kPrecise, bool kBatch>
 static void launch_force_t(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                            DevState* ds) {
     const int threads = 32 * L.warps_per_block;
     const size_t sm = (size_t)L.warps_per_block * sizeof(ForceSmem);
-    static int blocks[5] = {0, 0, 0, 0, 0};
-    int& nb = blocks[L.warps_per_block];
-    if (!nb) nb = resident_blocks(L, k_force<kIntegrate, kPrecise>, threads, sm);
-    k_force<kIntegrate, kPrecise><<<nb, threads, sm, L.stream>>>(c, b, ds);
+    static int blocks[5][8] = {};
+    int& nb = blocks[L.warps_per_block][L.blocks_per_sm & 7];
+    if (!nb) nb = resident_blocks(L, k_force<kIntegrate, kPrecise, kBatch>, threads, sm);
+    k_force<kIntegrate, kPrecise, kBatch><<<nb, threads, sm, L.stream>>>(c, b, ds);
 }
 
 int launch_force(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds,
                  int integrate) {
-    if (integrate) {
-        if (c.precise) launch_force_t<true, true>(L, c, b, ds);
-        else launch_force_t<true, false>(L, c, b, ds);
+    if (b.nscenes > 0) {
+        if (integrate) launch_force_t<true, false, true>(L, c, b, ds);
+        else launch_force_t<false, false, true>(L, c, b, ds);
+    } else if (integrate) {
+        if (c.precise) launch_force_t<true, true, false>(L, c, b, ds);
+        else launch_force_t<true, false, false>(L, c, b, ds);
     } else {
-        if (c.precise) launch_force_t<false, true>(L, c, b, ds);
-        else launch_force_t<false, false>(L, c, b, ds);
+        if (c.precise) launch_force_t<false, true, false>(L, c, b, ds);
+        else launch_force_t<false, false, false>(L, c, b, ds);
     }
     return 1;
 }

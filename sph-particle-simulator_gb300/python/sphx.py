@@ -34,7 +34,8 @@ EXPORTS = (
     "sphx_size", "sphx_get_time", "sphx_set_time", "sphx_get_stats", "sphx_reset_stats",
     "sphx_snapshot", "sphx_restore", "sphx_debug_pairs", "sphx_grid_create",
     "sphx_grid_destroy", "sphx_grid_build", "sphx_grid_query", "sphx_grid_info",
-    "sphx_grid_cell", "sphx_density_noalloc",
+    "sphx_grid_cell", "sphx_set_scenes", "sphx_get_scene_stats", "sphx_autotune",
+    "sphx_density_noalloc",
 )
 NOALLOC_MAX_PARTICLES = 65536
 
@@ -48,7 +49,14 @@ class SphxParams(C.Structure):
 
 class SphxTuning(C.Structure):
     _fields_ = [("mode", C.c_int), ("warps_per_block", C.c_int), ("blocks_per_sm", C.c_int),
-                ("max_grid_cells", C.c_int64), ("profile", C.c_int)]
+                ("max_grid_cells", C.c_int64), ("profile", C.c_int), ("graph", C.c_int)]
+
+
+class SphxSceneStats(C.Structure):
+    _fields_ = [("start", C.c_uint64), ("count", C.c_uint64), ("current_time", C.c_float),
+                ("last_dt", C.c_float), ("grid_cells", C.c_uint32), ("pad", C.c_uint32),
+                ("sum_mass", C.c_double), ("momentum", C.c_double * 3),
+                ("kinetic_energy", C.c_double), ("potential_energy", C.c_double)]
 
 
 class SphxStats(C.Structure):
@@ -108,6 +116,10 @@ def load_library(path: Path | str = LIB_PATH) -> C.CDLL:
         "sphx_restore": ([vp], C.c_int),
         "sphx_debug_pairs": ([vp, fp, fp, C.POINTER(sz)], C.c_int),
         "sphx_density_noalloc": ([C.POINTER(SphxParams), sz, fp, fp, fp, fp, vp], C.c_int),
+        "sphx_set_scenes": ([vp, C.c_uint32, fp, C.POINTER(SphxParams)], C.c_int),
+        "sphx_get_scene_stats": ([vp, C.c_uint32, C.POINTER(SphxSceneStats)], C.c_int),
+        "sphx_autotune": ([vp, C.c_float, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                           C.POINTER(C.c_float)], C.c_int),
         "sphx_grid_create": ([C.POINTER(vp), sz], C.c_int),
         "sphx_grid_destroy": ([vp], None),
         "sphx_grid_build": ([vp, sz, fp, C.c_float], C.c_int),
@@ -152,10 +164,12 @@ class Context:
     """One sphx context (one GPU step engine)."""
 
     def __init__(self, capacity: int, *, mode: int = MODE_EXACT, warps_per_block: int = 0,
-                 blocks_per_sm: int = 0, max_grid_cells: int = 0, profile: bool = False):
+                 blocks_per_sm: int = 0, max_grid_cells: int = 0, profile: bool = False,
+                 graph: bool = False):
         self._lib = lib()
         self._h = C.c_void_p()
-        t = SphxTuning(mode, warps_per_block, blocks_per_sm, max_grid_cells, int(profile))
+        t = SphxTuning(mode, warps_per_block, blocks_per_sm, max_grid_cells, int(profile),
+                       int(graph))
         self._check(self._lib.sphx_create(C.byref(self._h), capacity, C.byref(t)), "sphx_create")
         self.capacity = capacity
 
@@ -214,6 +228,27 @@ class Context:
         t, dt = C.c_double(), C.c_double()
         self._check(self._lib.sphx_get_time_f64(self._h, C.byref(t), C.byref(dt)), "sphx_get_time_f64")
         return t.value, dt.value
+
+    def set_scenes(self, scene_start, params_list):
+        """Split the loaded particles into scenes (contiguous ranges) with their parameters."""
+        ss = np.ascontiguousarray(scene_start, np.uint64)
+        k = ss.size - 1
+        arr = (SphxParams * max(k, 1))(*[params_struct(p) for p in params_list])
+        self._check(self._lib.sphx_set_scenes(self._h, k, _ptr(ss), arr), "sphx_set_scenes")
+
+    def autotune(self, dt: float) -> tuple[int, int, float]:
+        w, b, ms = C.c_int(), C.c_int(), C.c_float()
+        self._check(self._lib.sphx_autotune(self._h, C.c_float(dt), C.byref(w), C.byref(b),
+                                            C.byref(ms)), "sphx_autotune")
+        return w.value, b.value, ms.value
+
+    def scene_stats(self, scene: int) -> dict:
+        st = SphxSceneStats()
+        self._check(self._lib.sphx_get_scene_stats(self._h, scene, C.byref(st)),
+                    "sphx_get_scene_stats")
+        d = {name: getattr(st, name) for name, _ in st._fields_ if name != "pad"}
+        d["momentum"] = list(st.momentum)
+        return d
 
     def upload_ptr(self, n: int, pos_ptr: int, vel_ptr: int | None, mass_ptr: int):
         """Upload from raw host pointers (e.g. pinned buffers)."""

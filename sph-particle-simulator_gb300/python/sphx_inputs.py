@@ -174,4 +174,75 @@ def precision_cube(n: int = 1_000_000, seed: int = 2) -> Workload:
                     params=prm, dt=5e-4, steps=1, info=dict(seed=seed, periodic=1.0))
 
 
+@dataclass
+class Batch:
+    """Many independent scenes, concatenated in scene order."""
+    pos: np.ndarray          # (N, 3) float32
+    vel: np.ndarray          # (N, 3) float32
+    mass: np.ndarray         # (N,) float32
+    scene_start: np.ndarray  # (S + 1,) uint64
+    params: list             # S parameter blocks
+    dt: float
+    steps: int
+    info: list = field(default_factory=list)
+
+    @property
+    def n(self) -> int:
+        return int(self.pos.shape[0])
+
+    def scene(self, s: int):
+        a, b = int(self.scene_start[s]), int(self.scene_start[s + 1])
+        return self.pos[a:b], self.vel[a:b], self.mass[a:b], self.params[s]
+
+
+def fluid_drop_scene(target: int, r_frac: float, h_frac: float, v_down: float, seed: int,
+                     spacing: float = 0.01):
+    """A pool filling the bottom 30% of a cubic box plus a falling sphere, on a `spacing`
+    lattice with the dam break's jitter.  The box side L is chosen so that pool + sphere
+    hold about `target` particles: a pool of the bottom 30% of a *unit* box alone would
+    hold 300,000 particles at spacing 0.01, more than the largest scene, so the box (and
+    with it the sphere: radius r_frac * L, centre height h_frac * L) is scaled per scene."""
+    per_vol = 1.0 / spacing ** 3
+    L = (target / (per_vol * (0.3 + 4.0 / 3.0 * math.pi * r_frac ** 3))) ** (1.0 / 3.0)
+    nx = max(1, int(round(L / spacing)))
+    ny = max(1, int(round(0.3 * L / spacing)))
+    pool = lattice(nx, ny, nx, spacing=spacing, jitter=5e-4, seed=seed,
+                   origin=(spacing / 2, spacing / 2, spacing / 2))
+    R = r_frac * L
+    c = np.array([L / 2, h_frac * L, L / 2])
+    k = np.arange(-int(R / spacing) - 1, int(R / spacing) + 2)
+    gx, gy, gz = np.meshgrid(k, k, k, indexing="ij")
+    g = np.stack([gx.ravel(), gy.ravel(), gz.ravel()], axis=1).astype(np.float64) * spacing
+    sphere = (c + g[np.sum(g * g, axis=1) <= R * R]).astype(np.float32)
+    pos = np.concatenate([pool, sphere]).astype(np.float32)
+    vel = np.zeros_like(pos)
+    vel[pool.shape[0]:, 1] = -np.float32(v_down)
+    prm = params16(smoothing_length=0.02, neighbor_search_radius=0.04, particle_mass=1e-3,
+                   timestep=5e-4, xmin=0.0, xmax=L, ymin=0.0, ymax=L, zmin=0.0, zmax=L)
+    return pos, vel, prm, L
+
+
+def batched_fluid_drops(nscenes: int = 256, seed: int = 3, n_min: int = 2000,
+                        n_max: int = 200000) -> Batch:
+    """The batched fluid-drop mix: scene sizes log-uniform in [n_min, n_max] (about 11M
+    particles for 256 scenes), sphere radius U(0.05, 0.15), centre height U(0.6, 0.9) and
+    downward speed U(0, 2) m/s per scene (fractions of the scene's box), dt 5e-4."""
+    ids = np.arange(nscenes, dtype=np.uint64)
+    u = [uniform(seed, ids, k).astype(np.float64) for k in range(4)]
+    sizes = np.round(np.exp(np.log(n_min) + u[0] * (np.log(n_max) - np.log(n_min)))).astype(int)
+    P, V, params, info, start = [], [], [], [], [0]
+    for s in range(nscenes):
+        pos, vel, prm, L = fluid_drop_scene(int(sizes[s]), 0.05 + 0.10 * u[1][s],
+                                            0.6 + 0.3 * u[2][s], 2.0 * u[3][s], seed * 1000 + s)
+        P.append(pos)
+        V.append(vel)
+        params.append(prm)
+        info.append(dict(target=int(sizes[s]), n=int(pos.shape[0]), box=L))
+        start.append(start[-1] + pos.shape[0])
+    pos = np.concatenate(P)
+    return Batch(pos=pos, vel=np.concatenate(V), mass=np.full(pos.shape[0], 1e-3, np.float32),
+                 scene_start=np.array(start, np.uint64), params=params, dt=5e-4, steps=200,
+                 info=info)
+
+
 CONFIGS = {"dam_break_10k": config0, "dam_break_1M": config1, "dam_break_10M": config4}
