@@ -4,7 +4,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
+#include <utility>
 #include <vector>
 
 #include "sphx_internal.cuh"
@@ -97,6 +99,37 @@ float host_cubic_w(float sigma, float q) {
 
 void fill_step_const_from(sphx_ctx* c, const sphx_params& p, size_t n, StepConst& s);
 
+// Verifies the one-correction division sequence of xdiv_fixed for divisor b against IEEE
+// float division, for every dividend significand of the binade [1, 2) (about 8 ms).
+// Results are cached per divisor; only b in [2^-20, 2^20] qualifies.
+bool verify_fixed_divisor(float b) {
+    static std::mutex mu;
+    static std::vector<std::pair<uint32_t, bool>> cache;
+    if (!(b >= 0x1p-20f && b <= 0x1p20f)) return false;
+    uint32_t bits;
+    std::memcpy(&bits, &b, 4);
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        for (const auto& e : cache)
+            if (e.first == bits) return e.second;
+    }
+    const float y = 1.0f / b;
+    bool ok = true;
+    for (uint32_t m = 0; m < (1u << 23) && ok; ++m) {
+        const uint32_t abits = 0x3f800000u | m;
+        float a;
+        std::memcpy(&a, &abits, 4);
+        const float q0 = a * y;
+        const float r = std::fma(-q0, b, a);
+        const float q1 = std::fma(r, y, q0);
+        const float q = a / b;
+        ok = (q1 == q);
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    cache.emplace_back(bits, ok);
+    return ok;
+}
+
 void fill_step_const(sphx_ctx* c) { fill_step_const_from(c, c->params, c->n, c->sc); }
 
 void fill_step_const_from(sphx_ctx* c, const sphx_params& p, size_t n, StepConst& s) {
@@ -126,6 +159,10 @@ void fill_step_const_from(sphx_ctx* c, const sphx_params& p, size_t n, StepConst
     s.hi[1] = p.ymax;
     s.lo[2] = p.zmin;
     s.hi[2] = p.zmax;
+    s.rcp_h = 1.0f / h;
+    s.rcp_hsq = 1.0f / s.h_sq;
+    s.fast_div_h = verify_fixed_divisor(h) ? 1 : 0;
+    s.fast_div_hsq = verify_fixed_divisor(s.h_sq) ? 1 : 0;
     s.precise = c->tuning.mode != SPHX_MODE_EXACT;
     s.fp16 = c->tuning.mode == SPHX_MODE_PRECISE_FP16;
     s.cs = p.neighbor_search_radius;

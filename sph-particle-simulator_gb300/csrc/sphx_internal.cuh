@@ -41,6 +41,9 @@ struct StepConst {
     int fp16;              // 1: offsets rounded to binary16 at every write
     float cs;              // cell size of the storage and of the search grid (= r_search)
     double cs_d;           // the same, as double
+    // division by the fixed divisors h and h*h (see xdiv_fixed)
+    float rcp_h, rcp_hsq;  // RN(1/h), RN(1/h^2)
+    int fast_div_h, fast_div_hsq;  // 1: the one-correction sequence is verified for it
 };
 
 // Device-resident scalars written and read by the kernels of a step.
@@ -123,6 +126,25 @@ __device__ __forceinline__ float xsub(float a, float b) { return __fsub_rn(a, b)
 __device__ __forceinline__ float xdiv(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ float xsqrt(float a) { return __fsqrt_rn(a); }
 
+// a / b for a fixed divisor b, correctly rounded: q0 = RN(a*y), r = a - q0*b (exact, by
+// FMA), q = RN(q0 + r*y) with y = RN(1/b) -- Markstein's FMA correction (as in
+// Brisebarre, Muller & Raina, "Accelerating correctly rounded floating-point division
+// when the divisor is known in advance", IEEE TC 53(8), 2004).  The host verifies the
+// sequence for the divisor against IEEE division over every dividend significand of one
+// binade (`verified`); the sequence commutes with power-of-two scaling while every
+// intermediate stays normal, which |a| in [2^-60, 2^60] and b in [2^-20, 2^20] ensure.
+// Anything else (zero, subnormal, huge, NaN/inf dividend, unverified divisor) takes the
+// IEEE division.
+__device__ __forceinline__ float xdiv_fixed(float a, float b, float y, int verified) {
+    const float aa = fabsf(a);
+    if (verified && aa >= 0x1p-60f && aa <= 0x1p60f) {
+        const float q0 = __fmul_rn(a, y);
+        const float r = __fmaf_rn(-q0, b, a);
+        return __fmaf_rn(r, y, q0);
+    }
+    return __fdiv_rn(a, b);
+}
+
 // glm::dot(v, v) = (x*x + y*y) + z*z (products rounded first)
 __device__ __forceinline__ float xdot3(float x, float y, float z) {
     return xadd(xadd(xmul(x, x), xmul(y, y)), xmul(z, z));
@@ -160,10 +182,11 @@ __device__ __forceinline__ float cubic_grad_factor(const StepConst& c, float q) 
 // CubicSplineKernel::laplacianW_3d (kernels.cpp:130-138)
 __device__ __forceinline__ float cubic_lap(const StepConst& c, float q) {
     if (q >= 0.0f && q <= 1.0f) {
-        return xdiv(xmul(c.sigma, xadd(-2.0f, xmul(3.0f, q))), c.h_sq);
+        return xdiv_fixed(xmul(c.sigma, xadd(-2.0f, xmul(3.0f, q))), c.h_sq, c.rcp_hsq,
+                          c.fast_div_hsq);
     } else if (q > 1.0f && q <= 2.0f) {
         const float tmp = xsub(2.0f, q);
-        return xdiv(xmul(c.sigma, tmp), c.h_sq);
+        return xdiv_fixed(xmul(c.sigma, tmp), c.h_sq, c.rcp_hsq, c.fast_div_hsq);
     }
     return 0.0f;
 }

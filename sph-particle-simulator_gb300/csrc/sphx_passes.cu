@@ -372,7 +372,7 @@ __global__ void __launch_bounds__(128, 8) k_density(const StepConst cp, const Bu
                             S->tbuf[f - base] = xj.w * cubic_w_p(c, q);
                         } else {
                             const Diff d = diff(S->tpos[pr >> 5], xj);
-                            const float q = xdiv(xsqrt(d.d2), c.h);
+                            const float q = xdiv_fixed(xsqrt(d.d2), c.h, c.rcp_h, c.fast_div_h);
                             S->tbuf[f - base] = xmul(xj.w, cubic_w(c, q));
                         }
                     }
@@ -410,7 +410,8 @@ struct ForceSmem {
     float4 tpos[32], tvel[32];
     float tP[32];
     uint16_t plist[32 * 32];
-    float tb[6][kForceBatch];
+    float4 tbA[kForceBatch];  // pressure term x, y, z and viscosity term x
+    float2 tbB[kForceBatch];  // viscosity term y, z
     unsigned char skip[kForceBatch];
 };
 
@@ -424,7 +425,7 @@ __device__ __forceinline__ void force_term(const StepConst& c, const float4& xt,
                                            float* v3, bool& skip) {
     const Diff d = diff(xt, xj);
     const float r_len = xsqrt(d.d2);
-    const float q = xdiv(r_len, c.h);
+    const float q = xdiv_fixed(r_len, c.h, c.rcp_h, c.fast_div_h);
     skip = r_len < 1e-6f;
     p3[0] = p3[1] = p3[2] = 0.0f;
     if (!skip) {
@@ -437,9 +438,9 @@ __device__ __forceinline__ void force_term(const StepConst& c, const float4& xt,
             gz = xmul(gf, xdiv(d.z, r_len));
         }
         const float sp = xmul(xj.w, pt);
-        p3[0] = xmul(sp, xdiv(gx, c.h));
-        p3[1] = xmul(sp, xdiv(gy, c.h));
-        p3[2] = xmul(sp, xdiv(gz, c.h));
+        p3[0] = xmul(sp, xdiv_fixed(gx, c.h, c.rcp_h, c.fast_div_h));
+        p3[1] = xmul(sp, xdiv_fixed(gy, c.h, c.rcp_h, c.fast_div_h));
+        p3[2] = xmul(sp, xdiv_fixed(gz, c.h, c.rcp_h, c.fast_div_h));
     }
     const float lap = cubic_lap(c, q);
     const float sv = xmul(aj.w, c.visc);
@@ -587,32 +588,30 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buff
                             force_term(c, S->tpos[tt], S->tvel[tt], S->tP[tt], S->cpos[jj],
                                        S->cvel[jj], S->caux[jj], p3, v3, sk);
                         const uint32_t u = f - base;
-                        S->tb[0][u] = p3[0];
-                        S->tb[1][u] = p3[1];
-                        S->tb[2][u] = p3[2];
-                        S->tb[3][u] = v3[0];
-                        S->tb[4][u] = v3[1];
-                        S->tb[5][u] = v3[2];
+                        S->tbA[u] = make_float4(p3[0], p3[1], p3[2], v3[0]);
+                        S->tbB[u] = make_float2(v3[1], v3[2]);
                         S->skip[u] = sk;
                     }
                     __syncwarp();
                     const uint32_t k1 = min(o + cnt, end);
                     for (uint32_t k = max(o, base); k < k1; ++k) {
                         const uint32_t u = k - base;
+                        const float4 A = S->tbA[u];
+                        const float2 Bv = S->tbB[u];
                         if (kPrecise) {
-                            Fx.add(S->tb[3][u] - S->tb[0][u]);
-                            Fy.add(S->tb[4][u] - S->tb[1][u]);
-                            Fz.add(S->tb[5][u] - S->tb[2][u]);
+                            Fx.add(A.w - A.x);
+                            Fy.add(Bv.x - A.y);
+                            Fz.add(Bv.y - A.z);
                             continue;
                         }
                         if (!S->skip[u]) {
-                            fpx = xsub(fpx, S->tb[0][u]);
-                            fpy = xsub(fpy, S->tb[1][u]);
-                            fpz = xsub(fpz, S->tb[2][u]);
+                            fpx = xsub(fpx, A.x);
+                            fpy = xsub(fpy, A.y);
+                            fpz = xsub(fpz, A.z);
                         }
-                        fvx = xadd(fvx, S->tb[3][u]);
-                        fvy = xadd(fvy, S->tb[4][u]);
-                        fvz = xadd(fvz, S->tb[5][u]);
+                        fvx = xadd(fvx, A.w);
+                        fvy = xadd(fvy, Bv.x);
+                        fvz = xadd(fvz, Bv.y);
                     }
                     __syncwarp();
                 }
