@@ -190,7 +190,7 @@ void free_all(sphx_ctx* c) {
                     b.key[0], b.key[1], b.val[0], b.val[1],   b.key_s,     b.id_s,
                     b.off,  b.tile_start, b.hist, b.scan_part, b.diag_part, c->ds,
                     c->stage, c->snap_pos, c->snap_vel, c->snap_cell, b.cell4, b.cell4_s,
-                    b.scene_of, b.scene_s, b.scenes};
+                    b.scene_of, b.scene_s, b.scenes, b.hitmask, b.tile_slot};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto& slot : c->prof)
@@ -400,6 +400,22 @@ int sphx_create(sphx_ctx** out, size_t capacity, const sphx_tuning* tuning) {
     if (c->tuning.mode != SPHX_MODE_EXACT &&
         ((rc = dmalloc(&b.cell4, C)) || (rc = dmalloc(&b.cell4_s, C))))
         return fail(rc);
+    // Hit-mask pool: 3 records (128 B each) per particle of capacity covers the 27-cell
+    // stencil of dense states (about 2 chunks per particle-tile row set); without it (or
+    // when a step needs more) the force pass repeats the distance tests.
+    if (dmalloc(&b.tile_slot, C) == SPHX_OK) {
+        unsigned long long cap = 3ull * C;
+        if (cap > 0xffff0000ull) cap = 0xffff0000ull;  // record indices are 32-bit
+        if (dmalloc(&b.hitmask, (size_t)cap * 32) == SPHX_OK) {
+            b.hitmask_cap = cap;
+        } else {
+            cudaGetLastError();
+            cudaFree(b.tile_slot);
+            b.tile_slot = nullptr;
+        }
+    } else {
+        cudaGetLastError();
+    }
     if (cudaMemset(c->ds, 0, sizeof(DevState)) != cudaSuccess) return fail(SPHX_ERR_CUDA);
     if (cudaMemset(b.aux4_s, 0, C * sizeof(float4)) != cudaSuccess ||
         cudaMemset(b.acc4_s, 0, C * sizeof(float4)) != cudaSuccess)

@@ -60,6 +60,7 @@ struct DevState {
     uint32_t occupied;          // occupied cells
     uint32_t max_occ;           // particles in the fullest cell
     uint32_t work[2];           // tile counters of the density and force passes
+    unsigned long long mask_used;  // hit-mask records reserved by the density pass
     float dt;                   // dt of the current step
     float time;                 // current_time_
     float a0[4];                // accelerations_[0] (persists across steps)
@@ -114,10 +115,19 @@ struct Buffers {
     uint32_t* scene_s;   // batched mode: scene of each particle (cell-sorted)
     SceneInfo* scenes;   // batched mode: per-scene records
     int nscenes;         // 0: single scene
+    // Hit masks of the density pass, reused by the force pass of the same step: record r
+    // holds 32 words (word = lane: bit j set if candidate j of the chunk is within r of the
+    // lane's particle).  Each tile reserves one record per chunk of its walk;
+    // tile_slot[t] = first record, or kNoSlot when the pool had no room (the force pass
+    // then repeats the distance tests for that tile).
+    uint32_t* hitmask = nullptr;
+    uint32_t* tile_slot = nullptr;
+    unsigned long long hitmask_cap = 0;  // records
     int radix_blocks;
     int scan_part_cap;
     int diag_blocks;
 };
+constexpr uint32_t kNoSlot = 0xffffffffu;
 
 // ---- exact float arithmetic: IEEE round-to-nearest, never contracted into FMA ---------
 __device__ __forceinline__ float xmul(float a, float b) { return __fmul_rn(a, b); }

@@ -224,6 +224,29 @@ __device__ __forceinline__ uint32_t warp_excl_scan(uint32_t v, int lane, uint32_
     return x - v;
 }
 
+// Number of chunks of the tile's walk (the row segments cut into runs of kTile).
+__device__ __forceinline__ uint32_t walk_chunks(const Buffers& b, const Geom& g, const Tile& T) {
+    uint32_t n = 0;
+    for_each_row(b, g, T, [&](int a, int e) { n += (uint32_t)(e - a + kTile - 1) / kTile; });
+    return n;
+}
+
+// Density pass: reserves one hit-mask record per chunk of tile t's walk (kNoSlot when the
+// pool has no room) and publishes it for the force pass.
+__device__ __forceinline__ uint32_t reserve_hit_masks(const Buffers& b, const Geom& g,
+                                                      const Tile& T, uint32_t t, int lane,
+                                                      DevState* ds) {
+    if (!b.hitmask) return kNoSlot;
+    const uint32_t nch = walk_chunks(b, g, T);
+    uint32_t slot = kNoSlot;
+    if (lane == 0) {
+        const unsigned long long s0 = atomicAdd(&ds->mask_used, (unsigned long long)nch);
+        if (s0 + nch <= b.hitmask_cap) slot = (uint32_t)s0;
+        b.tile_slot[t] = slot;
+    }
+    return __shfl_sync(kFull, slot, 0);
+}
+
 // Axis-aligned box of the tile's particles (valid lanes).
 struct TileBox {
     float lo[3], hi[3];
@@ -339,8 +362,10 @@ __global__ void __launch_bounds__(128, 8) k_density(const StepConst cp, const Bu
         KSum rk;
         rk.s = rho;
         uint32_t nn = 0;
+        const uint32_t slot = reserve_hit_masks(b, g, T, t, lane, ds);
+        uint32_t* rec = slot != kNoSlot ? b.hitmask + (size_t)slot * 32 + lane : nullptr;
         for_each_row(b, g, T, [&](int a, int e) {
-            for (int s = a; s < e; s += kTile) {
+            for (int s = a; s < e; s += kTile, rec += rec ? 32 : 0) {
                 const int m = min(kTile, e - s);
                 __syncwarp();
                 float4 pl = lane < m ? b.pos4_s[s + lane] : make_float4(inf, inf, inf, 0.f);
@@ -348,8 +373,12 @@ __global__ void __launch_bounds__(128, 8) k_density(const StepConst cp, const Bu
                 S->cand[lane] = pl;
                 const uint32_t surv = __ballot_sync(kFull, box_near(B, pl, r2m));
                 __syncwarp();
-                if (!surv) continue;
+                if (!surv) {
+                    if (rec) *rec = 0u;
+                    continue;
+                }
                 uint32_t mask = valid ? chunk_hits<kPrecise>(S->cand, surv, xi, c.r2) : 0u;
+                if (rec) *rec = mask;
                 nn += __popc(mask);
                 const int self = i - s;
                 if ((unsigned)self < 32u) mask &= ~(1u << self);
@@ -406,27 +435,28 @@ __global__ void __launch_bounds__(128, 8) k_density(const StepConst cp, const Bu
 //  ParticleSystem::apply_boundary_conditions, particle.cpp:122-153)
 // ---------------------------------------------------------------------------------------
 struct ForceSmem {
+    float4 box_lo, box_hi;  // tile box (the fallback walk's culling test)
     float4 cpos[32], cvel[32], caux[32];
     float4 tpos[32], tvel[32];
     float tP[32];
     uint16_t plist[32 * 32];
     float4 tbA[kForceBatch];  // pressure term x, y, z and viscosity term x
     float2 tbB[kForceBatch];  // viscosity term y, z
-    unsigned char skip[kForceBatch];
 };
 
 // The pair term of particle t against candidate j: the pressure-force contribution
-// m_j * (P_t + P_j)/(2 rho_j) * gradW (subtracted by the caller; skipped when
-// |r| < 1e-6) and the viscosity contribution ((m_j/rho_j) mu (v_j - v_t)) laplacianW
-// (added), each with the reference's operations.
+// m_j * (P_t + P_j)/(2 rho_j) * gradW (subtracted by the caller; +0 when |r| < 1e-6,
+// where the reference skips it: subtracting +0 leaves every float unchanged) and the
+// viscosity contribution ((m_j/rho_j) mu (v_j - v_t)) laplacianW (added), each with the
+// reference's operations.
 __device__ __forceinline__ void force_term(const StepConst& c, const float4& xt,
                                            const float4& vt, float Pt, const float4& xj,
                                            const float4& vj, const float4& aj, float* p3,
-                                           float* v3, bool& skip) {
+                                           float* v3) {
     const Diff d = diff(xt, xj);
     const float r_len = xsqrt(d.d2);
     const float q = xdiv_fixed(r_len, c.h, c.rcp_h, c.fast_div_h);
-    skip = r_len < 1e-6f;
+    const bool skip = r_len < 1e-6f;
     p3[0] = p3[1] = p3[2] = 0.0f;
     if (!skip) {
         const float pt = xdiv(xadd(Pt, aj.y), aj.z);
@@ -453,11 +483,11 @@ __device__ __forceinline__ void force_term(const StepConst& c, const float4& xt,
 __device__ __forceinline__ void force_term_p(const StepConst& c, const float4& xt,
                                              const float4& vt, float Pt, const float4& xj,
                                              const float4& vj, const float4& aj, float* p3,
-                                             float* v3, bool& skip) {
+                                             float* v3) {
     const float dx = xt.x - xj.x, dy = xt.y - xj.y, dz = xt.z - xj.z;
     const float r_len = sqrtf(dx * dx + dy * dy + dz * dz);
     const float q = r_len / c.h;
-    skip = r_len < 1e-6f;
+    const bool skip = r_len < 1e-6f;
     p3[0] = p3[1] = p3[2] = 0.0f;
     if (!skip) {
         float gf = 0.0f;
@@ -531,7 +561,6 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buff
         const int scene = kBatch ? (int)b.scene_s[k0] : 0;
         const StepConst& c = kBatch ? b.scenes[scene].c : cp;
         const Geom g = kBatch ? scene_geom(b.scenes[scene], ds) : grid_geom(ds);
-        const float dt = kBatch ? b.scenes[scene].dt : ds->dt;
         const float r2m = c.r2 * 1.0001f;
         Tile T;
         float4 xi;
@@ -540,31 +569,60 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buff
         if (kPrecise) tile_setup_cells(c, b, g, k0, lane, T, xi, valid, frame);
         else tile_setup(c, b, g, k0, lane, T, xi, valid);
         const int i = T.k0 + lane;
-        const float4 vi = valid ? b.vel4_s[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 vi0 = valid ? b.vel4_s[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float Pi = valid ? b.aux4_s[i].y : 0.0f;
-        const TileBox B = tile_box(xi, valid);
+        // hit masks of the density pass (same walk, same chunks, same tests)
+        const uint32_t slot = b.tile_slot ? b.tile_slot[t] : kNoSlot;
+        if (slot == kNoSlot) {
+            const TileBox B = tile_box(xi, valid);
+            if (lane == 0) {
+                S->box_lo = make_float4(B.lo[0], B.lo[1], B.lo[2], 0.0f);
+                S->box_hi = make_float4(B.hi[0], B.hi[1], B.hi[2], 0.0f);
+            }
+        }
         S->tpos[lane] = xi;
-        S->tvel[lane] = vi;
+        S->tvel[lane] = vi0;
         S->tP[lane] = Pi;
         float fpx = 0.0f, fpy = 0.0f, fpz = 0.0f;
         float fvx = 0.0f, fvy = 0.0f, fvz = 0.0f;
         KSum Fx, Fy, Fz;  // precision mode: one compensated sum per component
+        const uint32_t* rec = slot != kNoSlot ? b.hitmask + (size_t)slot * 32 + lane : nullptr;
         for_each_row(b, g, T, [&](int a, int e) {
-            for (int s = a; s < e; s += kTile) {
+            for (int s = a; s < e; s += kTile, rec += rec ? 32 : 0) {
                 const int m = min(kTile, e - s);
+                uint32_t mask;
                 __syncwarp();
-                const bool in = lane < m;
-                float4 pl = in ? b.pos4_s[s + lane] : make_float4(inf, inf, inf, 0.f);
-                if (kPrecise && in) pl = frame_pos(b.cell4_s[s + lane], frame, pl, c.cs);
-                S->cpos[lane] = pl;
-                const uint32_t surv = __ballot_sync(kFull, box_near(B, pl, r2m));
-                if (!surv) continue;
-                if (surv & (1u << lane)) {
-                    S->cvel[lane] = b.vel4_s[s + lane];
-                    S->caux[lane] = b.aux4_s[s + lane];
+                if (rec) {
+                    mask = *rec;
+                    const uint32_t used = __reduce_or_sync(kFull, mask);  // candidates hit
+                    if (!used) continue;
+                    if (used & (1u << lane)) {
+                        float4 pl = b.pos4_s[s + lane];
+                        if (kPrecise) pl = frame_pos(b.cell4_s[s + lane], frame, pl, c.cs);
+                        S->cpos[lane] = pl;
+                        S->cvel[lane] = b.vel4_s[s + lane];
+                        S->caux[lane] = b.aux4_s[s + lane];
+                    }
+                    __syncwarp();
+                } else {
+                    const bool in = lane < m;
+                    float4 pl = in ? b.pos4_s[s + lane] : make_float4(inf, inf, inf, 0.f);
+                    if (kPrecise && in) pl = frame_pos(b.cell4_s[s + lane], frame, pl, c.cs);
+                    S->cpos[lane] = pl;
+                    __syncwarp();
+                    TileBox B;
+                    const float4 lo = S->box_lo, hi = S->box_hi;
+                    B.lo[0] = lo.x, B.lo[1] = lo.y, B.lo[2] = lo.z;
+                    B.hi[0] = hi.x, B.hi[1] = hi.y, B.hi[2] = hi.z;
+                    const uint32_t surv = __ballot_sync(kFull, box_near(B, pl, r2m));
+                    if (!surv) continue;
+                    if (surv & (1u << lane)) {
+                        S->cvel[lane] = b.vel4_s[s + lane];
+                        S->caux[lane] = b.aux4_s[s + lane];
+                    }
+                    __syncwarp();
+                    mask = valid ? chunk_hits<kPrecise>(S->cpos, surv, xi, c.r2) : 0u;
                 }
-                __syncwarp();
-                uint32_t mask = valid ? chunk_hits<kPrecise>(S->cpos, surv, xi, c.r2) : 0u;
                 const int self = i - s;
                 if ((unsigned)self < 32u) mask &= ~(1u << self);
                 const uint32_t cnt = __popc(mask);
@@ -580,17 +638,15 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buff
                         const uint32_t pr = S->plist[f];
                         const int tt = pr >> 5, jj = pr & 31;
                         float p3[3], v3[3];
-                        bool sk;
                         if (kPrecise)
                             force_term_p(c, S->tpos[tt], S->tvel[tt], S->tP[tt], S->cpos[jj],
-                                         S->cvel[jj], S->caux[jj], p3, v3, sk);
+                                         S->cvel[jj], S->caux[jj], p3, v3);
                         else
                             force_term(c, S->tpos[tt], S->tvel[tt], S->tP[tt], S->cpos[jj],
-                                       S->cvel[jj], S->caux[jj], p3, v3, sk);
+                                       S->cvel[jj], S->caux[jj], p3, v3);
                         const uint32_t u = f - base;
                         S->tbA[u] = make_float4(p3[0], p3[1], p3[2], v3[0]);
                         S->tbB[u] = make_float2(v3[1], v3[2]);
-                        S->skip[u] = sk;
                     }
                     __syncwarp();
                     const uint32_t k1 = min(o + cnt, end);
@@ -604,11 +660,10 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buff
                             Fz.add(Bv.y - A.z);
                             continue;
                         }
-                        if (!S->skip[u]) {
-                            fpx = xsub(fpx, A.x);
-                            fpy = xsub(fpy, A.y);
-                            fpz = xsub(fpz, A.z);
-                        }
+                        // a skipped pressure term is +0, and x - (+0) == x exactly
+                        fpx = xsub(fpx, A.x);
+                        fpy = xsub(fpy, A.y);
+                        fpz = xsub(fpz, A.z);
                         fvx = xadd(fvx, A.w);
                         fvy = xadd(fvy, Bv.x);
                         fvz = xadd(fvz, Bv.y);
@@ -632,6 +687,8 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buff
         }
         b.acc4_s[i] = make_float4(ax, ay, az, 0.0f);
         if (!kIntegrate) continue;
+        const float dt = kBatch ? b.scenes[scene].dt : ds->dt;
+        const float4 vi = S->tvel[lane];
         const uint32_t id = b.id_s[i];
         if (kPrecise) {
             int4 cell = b.cell4_s[i];
