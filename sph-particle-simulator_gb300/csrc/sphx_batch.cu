@@ -29,7 +29,6 @@ __global__ void k_batch_begin(SceneInfo* scenes, int nscenes, DevState* ds) {
         ds->n_tiles = 0;
         ds->work[0] = 0;
         ds->work[1] = 0;
-        ds->mask_used = 0ull;
     }
     if (s >= nscenes) return;
     SceneInfo& sc = scenes[s];

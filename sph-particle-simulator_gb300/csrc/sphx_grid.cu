@@ -39,7 +39,6 @@ __global__ void k_begin_step(DevState* ds, int reset_bbox) {
     ds->n_tiles = 0;
     ds->work[0] = 0;
     ds->work[1] = 0;
-    ds->mask_used = 0ull;
 }
 
 int launch_begin_step(const LaunchCtx& L, DevState* ds, int reset_bbox) {

@@ -60,7 +60,6 @@ struct DevState {
     uint32_t occupied;          // occupied cells
     uint32_t max_occ;           // particles in the fullest cell
     uint32_t work[2];           // tile counters of the density and force passes
-    unsigned long long mask_used;  // hit-mask records reserved by the density pass
     float dt;                   // dt of the current step
     float time;                 // current_time_
     float a0[4];                // accelerations_[0] (persists across steps)
@@ -117,9 +116,10 @@ struct Buffers {
     int nscenes;         // 0: single scene
     // Hit masks of the density pass, reused by the force pass of the same step: record r
     // holds 32 words (word = lane: bit j set if candidate j of the chunk is within r of the
-    // lane's particle).  Each tile reserves one record per chunk of its walk;
-    // tile_slot[t] = first record, or kNoSlot when the pool had no room (the force pass
-    // then repeats the distance tests for that tile).
+    // lane's particle).  Every warp of the density grid owns an equal region of the pool
+    // and stores its tiles' records one after another, one record per chunk of the tile's
+    // walk; tile_slot[t] = first record, or kNoSlot when the tile did not fit in what was
+    // left of the region (the force pass then repeats the distance tests for that tile).
     uint32_t* hitmask = nullptr;
     uint32_t* tile_slot = nullptr;
     unsigned long long hitmask_cap = 0;  // records

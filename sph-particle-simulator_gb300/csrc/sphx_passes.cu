@@ -224,29 +224,6 @@ __device__ __forceinline__ uint32_t warp_excl_scan(uint32_t v, int lane, uint32_
     return x - v;
 }
 
-// Number of chunks of the tile's walk (the row segments cut into runs of kTile).
-__device__ __forceinline__ uint32_t walk_chunks(const Buffers& b, const Geom& g, const Tile& T) {
-    uint32_t n = 0;
-    for_each_row(b, g, T, [&](int a, int e) { n += (uint32_t)(e - a + kTile - 1) / kTile; });
-    return n;
-}
-
-// Density pass: reserves one hit-mask record per chunk of tile t's walk (kNoSlot when the
-// pool has no room) and publishes it for the force pass.
-__device__ __forceinline__ uint32_t reserve_hit_masks(const Buffers& b, const Geom& g,
-                                                      const Tile& T, uint32_t t, int lane,
-                                                      DevState* ds) {
-    if (!b.hitmask) return kNoSlot;
-    const uint32_t nch = walk_chunks(b, g, T);
-    uint32_t slot = kNoSlot;
-    if (lane == 0) {
-        const unsigned long long s0 = atomicAdd(&ds->mask_used, (unsigned long long)nch);
-        if (s0 + nch <= b.hitmask_cap) slot = (uint32_t)s0;
-        b.tile_slot[t] = slot;
-    }
-    return __shfl_sync(kFull, slot, 0);
-}
-
 // Axis-aligned box of the tile's particles (valid lanes).
 struct TileBox {
     float lo[3], hi[3];
@@ -327,6 +304,8 @@ __device__ __forceinline__ uint32_t next_tile(uint32_t* ctr, int lane) {
 // (compute_density / compute_pressure, sph_engine.cpp:370-388)
 // ---------------------------------------------------------------------------------------
 struct DensitySmem {
+    float4 box_lo, box_hi;  // tile box (culling test)
+    uint32_t mcur, mend;    // the warp's region of the hit-mask pool: [mcur, mend)
     float4 cand[32];
     float4 tpos[32];
     uint16_t plist[32 * 32];
@@ -341,6 +320,15 @@ __global__ void __launch_bounds__(128, 8) k_density(const StepConst cp, const Bu
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     DensitySmem* S = reinterpret_cast<DensitySmem*>(smem_raw_d) + warp;
     const uint32_t ntiles = ds->n_tiles;
+    // this warp's region of the hit-mask pool, filled tile after tile (record indices fit
+    // 32 bits: the pool holds at most 0xffff0000 records)
+    if (lane == 0) {
+        const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+        const uint32_t region = b.hitmask ? (uint32_t)(b.hitmask_cap / nwarps) : 0u;
+        S->mcur = (blockIdx.x * (blockDim.x >> 5) + warp) * region;
+        S->mend = S->mcur + region;
+    }
+    __syncwarp();
     const float inf = __int_as_float(0x7f800000);
     uint32_t my_max = 0;
     for (uint32_t t = next_tile(&ds->work[0], lane); t < ntiles; t = next_tile(&ds->work[0], lane)) {
@@ -356,29 +344,46 @@ __global__ void __launch_bounds__(128, 8) k_density(const StepConst cp, const Bu
         if (kPrecise) tile_setup_cells(c, b, g, k0, lane, T, xi, valid, frame);
         else tile_setup(c, b, g, k0, lane, T, xi, valid);
         const int i = T.k0 + lane;
-        const TileBox B = tile_box(xi, valid);
+        {
+            const TileBox B = tile_box(xi, valid);
+            if (lane == 0) {
+                S->box_lo = make_float4(B.lo[0], B.lo[1], B.lo[2], 0.0f);
+                S->box_hi = make_float4(B.hi[0], B.hi[1], B.hi[2], 0.0f);
+            }
+        }
         S->tpos[lane] = xi;
         float rho = xmul(xi.w, c.w0);
         KSum rk;
         rk.s = rho;
         uint32_t nn = 0;
-        const uint32_t slot = reserve_hit_masks(b, g, T, t, lane, ds);
-        uint32_t* rec = slot != kNoSlot ? b.hitmask + (size_t)slot * 32 + lane : nullptr;
+        // hit-mask records of this tile: from the warp's cursor on, one per chunk
+        __syncwarp();
+        const uint32_t slot = S->mcur, room = S->mend - slot;
+        uint32_t nrec = 0;
         for_each_row(b, g, T, [&](int a, int e) {
-            for (int s = a; s < e; s += kTile, rec += rec ? 32 : 0) {
+            for (int s = a; s < e; s += kTile, ++nrec) {
                 const int m = min(kTile, e - s);
                 __syncwarp();
                 float4 pl = lane < m ? b.pos4_s[s + lane] : make_float4(inf, inf, inf, 0.f);
                 if (kPrecise && lane < m) pl = frame_pos(b.cell4_s[s + lane], frame, pl, c.cs);
                 S->cand[lane] = pl;
+                TileBox B;
+                {
+                    const float4 lo = S->box_lo, hi = S->box_hi;
+                    B.lo[0] = lo.x, B.lo[1] = lo.y, B.lo[2] = lo.z;
+                    B.hi[0] = hi.x, B.hi[1] = hi.y, B.hi[2] = hi.z;
+                }
                 const uint32_t surv = __ballot_sync(kFull, box_near(B, pl, r2m));
                 __syncwarp();
+                uint32_t* rec =
+                    nrec < room ? b.hitmask + (size_t)(slot + nrec) * 32 + lane : nullptr;
+                // streaming stores: the records must not evict the candidate arrays from L2
                 if (!surv) {
-                    if (rec) *rec = 0u;
+                    if (rec) __stcs(rec, 0u);
                     continue;
                 }
                 uint32_t mask = valid ? chunk_hits<kPrecise>(S->cand, surv, xi, c.r2) : 0u;
-                if (rec) *rec = mask;
+                if (rec) __stcs(rec, mask);
                 nn += __popc(mask);
                 const int self = i - s;
                 if ((unsigned)self < 32u) mask &= ~(1u << self);
@@ -415,6 +420,11 @@ __global__ void __launch_bounds__(128, 8) k_density(const StepConst cp, const Bu
                 }
             }
         });
+        if (b.hitmask && lane == 0) {
+            const bool fits = nrec <= room;
+            b.tile_slot[t] = fits ? slot : kNoSlot;
+            if (fits) S->mcur = slot + nrec;
+        }
         if (valid) {
             if (kPrecise) rho = rk.value();
             const float P = xmul(c.gas, xsub(rho, c.rest));
@@ -593,7 +603,7 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buff
                 uint32_t mask;
                 __syncwarp();
                 if (rec) {
-                    mask = *rec;
+                    mask = __ldcs(rec);  // read once
                     const uint32_t used = __reduce_or_sync(kFull, mask);  // candidates hit
                     if (!used) continue;
                     if (used & (1u << lane)) {
