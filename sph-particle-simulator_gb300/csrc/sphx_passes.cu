@@ -182,6 +182,73 @@ __device__ __forceinline__ void for_each_row(const Buffers& b, const Geom& g, co
     }
 }
 
+// The same walk as for_each_row, listed up front: writes the tile's non-empty row
+// segments [a, e) to seg in visiting order and returns their number (<= 75: 5 x 5 rows of
+// up to 3 pieces).  One lane per row (dx, dy) -- lane order is the rows' visiting order --
+// and a warp scan places each row's pieces.
+constexpr int kMaxSegments = 75;
+__device__ __forceinline__ int build_segments(const Buffers& b, const Geom& g, const Tile& T,
+                                              int lane, int2* seg) {
+    if (!T.cells) return 0;
+    const int d0 = g.dim[0], d1 = g.dim[1], d2 = g.dim[2];
+    int z0 = T.cz + T.lo[2], z1 = T.cz + T.hi[2], z2 = -1;
+    int zp = -1, zq = -2;
+    if (g.wrap[2]) {
+        if (z0 < 0) {
+            zp = z0 + d2;
+            zq = d2 - 1;
+            z0 = 0;
+        }
+        if (z1 >= d2) {
+            z2 = z1 - d2;
+            z1 = d2 - 1;
+        }
+    } else {
+        z0 = max(z0, 0);
+        z1 = min(z1, d2 - 1);
+    }
+    const int ny = T.hi[1] - T.lo[1] + 1;
+    const int nrows = (T.hi[0] - T.lo[0] + 1) * ny;
+    int2 p0 = make_int2(0, 0), p1 = p0, p2 = p0;  // the row's pieces, in dz order
+    bool v0 = false, v1 = false, v2 = false;
+    if (lane < nrows) {
+        int X = T.cx + T.lo[0] + lane / ny;
+        int Y = T.cy + T.lo[1] + lane % ny;
+        bool ok = true;
+        if (g.wrap[0]) X = (X + d0) % d0;
+        else ok = X >= 0 && X < d0;
+        if (g.wrap[1]) Y = (Y + d1) % d1;
+        else ok = ok && Y >= 0 && Y < d1;
+        if (ok) {
+            const uint32_t rb = g.base + ((uint32_t)X * (uint32_t)d1 + (uint32_t)Y) * (uint32_t)d2;
+            if (zp <= zq) {
+                p0 = make_int2((int)b.off[rb + zp], (int)b.off[rb + zq + 1]);
+                v0 = p0.x < p0.y;
+            }
+            if (z0 <= z1) {
+                p1 = make_int2((int)b.off[rb + z0], (int)b.off[rb + z1 + 1]);
+                v1 = p1.x < p1.y;
+            }
+            if (z2 >= 0) {
+                p2 = make_int2((int)b.off[rb], (int)b.off[rb + z2 + 1]);
+                v2 = p2.x < p2.y;
+            }
+        }
+    }
+    const uint32_t np = (uint32_t)v0 + (uint32_t)v1 + (uint32_t)v2;
+    uint32_t x = np;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    uint32_t at = x - np;
+    if (v0) seg[at++] = p0;
+    if (v1) seg[at++] = p1;
+    if (v2) seg[at] = p2;
+    return (int)__shfl_sync(0xffffffffu, x, 31);
+}
+
 // d = x_i - x_j; d2 = dot(d, d)  (spatial_hash.h:70-73, sph_engine.cpp:378, 400, 424)
 struct Diff {
     float x, y, z, d2;
@@ -306,6 +373,7 @@ __device__ __forceinline__ uint32_t next_tile(uint32_t* ctr, int lane) {
 struct DensitySmem {
     float4 box_lo, box_hi;  // tile box (culling test)
     uint32_t mcur, mend;    // the warp's region of the hit-mask pool: [mcur, mend)
+    int2 seg[kMaxSegments]; // the tile's row segments
     float4 cand[32];
     float4 tpos[32];
     uint16_t plist[32 * 32];
@@ -360,7 +428,11 @@ __global__ void __launch_bounds__(128, 8) k_density(const StepConst cp, const Bu
         __syncwarp();
         const uint32_t slot = S->mcur, room = S->mend - slot;
         uint32_t nrec = 0;
-        for_each_row(b, g, T, [&](int a, int e) {
+        const int nseg = build_segments(b, g, T, lane, S->seg);
+        __syncwarp();
+        for (int sg = 0; sg < nseg; ++sg) {
+            const int2 se = S->seg[sg];
+            const int a = se.x, e = se.y;
             for (int s = a; s < e; s += kTile, ++nrec) {
                 const int m = min(kTile, e - s);
                 __syncwarp();
@@ -419,7 +491,7 @@ __global__ void __launch_bounds__(128, 8) k_density(const StepConst cp, const Bu
                     __syncwarp();
                 }
             }
-        });
+        }
         if (b.hitmask && lane == 0) {
             const bool fits = nrec <= room;
             b.tile_slot[t] = fits ? slot : kNoSlot;
@@ -446,6 +518,7 @@ __global__ void __launch_bounds__(128, 8) k_density(const StepConst cp, const Bu
 // ---------------------------------------------------------------------------------------
 struct ForceSmem {
     float4 box_lo, box_hi;  // tile box (the fallback walk's culling test)
+    int2 seg[kMaxSegments]; // the tile's row segments
     float4 cpos[32], cvel[32], caux[32];
     float4 tpos[32], tvel[32];
     float tP[32];
@@ -597,7 +670,11 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buff
         float fvx = 0.0f, fvy = 0.0f, fvz = 0.0f;
         KSum Fx, Fy, Fz;  // precision mode: one compensated sum per component
         const uint32_t* rec = slot != kNoSlot ? b.hitmask + (size_t)slot * 32 + lane : nullptr;
-        for_each_row(b, g, T, [&](int a, int e) {
+        const int nseg = build_segments(b, g, T, lane, S->seg);
+        __syncwarp();
+        for (int sg = 0; sg < nseg; ++sg) {
+            const int2 se = S->seg[sg];
+            const int a = se.x, e = se.y;
             for (int s = a; s < e; s += kTile, rec += rec ? 32 : 0) {
                 const int m = min(kTile, e - s);
                 uint32_t mask;
@@ -681,7 +758,7 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buff
                     __syncwarp();
                 }
             }
-        });
+        }
         __syncwarp();
         if (!valid) continue;
         const float mi = xi.w;
