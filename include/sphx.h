@@ -67,6 +67,11 @@ typedef struct sphx_params {
 #define SPHX_MODE_PRECISE 1
 #define SPHX_MODE_PRECISE_FP16 2 /* as PRECISE, offsets rounded to binary16 at every write */
 
+/* Smoothing kernels, numbered as sph::KernelType (src/kernels.h:94-98). */
+#define SPHX_KERNEL_CUBIC_SPLINE 0 /* CubicSplineKernel, the reference engine's choice */
+#define SPHX_KERNEL_WENDLAND_C2 1  /* WendlandC2Kernel (src/kernels.cpp:166-200) */
+#define SPHX_KERNEL_GAUSSIAN 2     /* GaussianKernel (src/kernels.cpp:203-225) */
+
 typedef struct sphx_tuning {
     int mode;              /* SPHX_MODE_* (default EXACT) */
     int warps_per_block;   /* neighbour-pass CTA size in warps; 0 = default (4) */
@@ -124,6 +129,18 @@ int sphx_set_stream(sphx_ctx* ctx, void* cuda_stream);
  * uses params exactly as given (search radius = neighbor_search_radius; the 2h rule of
  * set_smoothing_length is the host engine's business). */
 int sphx_set_params(sphx_ctx* ctx, const sphx_params* params);
+
+/* Smoothing kernel of the density and force passes: the kernel create_kernel(kernel, h)
+ * returns (src/kernels.cpp:226-236), evaluated per pair through the equations:: formulas
+ * (src/sph_engine.cpp:370-432).  The reference engine itself always uses the cubic spline
+ * (src/sph_engine.cpp:17, 23, 162); the other two are reachable there only through
+ * create_kernel + equations::*, and this call is how the drop-in reaches them.  Unknown
+ * kernel -> SPHX_ERR_INVALID_ARG (create_kernel throws std::invalid_argument,
+ * kernels.cpp:233-234).  Cubic spline and Wendland C2 results are bit-identical to the
+ * reference's; the Gaussian's exp is CUDA's expf (max 2 ulp) where the reference calls
+ * the C library's expf, so its terms may differ in the last bits. */
+int sphx_set_kernel(sphx_ctx* ctx, int kernel);
+int sphx_get_kernel(sphx_ctx* ctx, int* kernel);
 
 /* Replaces the particle set with n particles from host memory (the device side of
  * SPHEngine::add_particles / clear_particles, src/sph_engine.cpp:83-91).  vel may be NULL

@@ -112,15 +112,16 @@ int64_t ref_query(size_t n, const float* pos, float cell_size, float radius,
 }
 
 // One evaluation of the step's field phases on a given state, through the reference's
-// own equations:: functions and cubic-spline kernel (the loop bodies of
-// compute_densities / compute_pressures / compute_forces, src/sph_engine.cpp:203-244).
-// Writes rho[n], P[n], acc[3n].
-void ref_fields(size_t n, const float* pos, const float* vel, const float* mass,
-                const float* params16, float* rho, float* P, float* acc) {
+// own equations:: functions and the kernel create_kernel(kind, h) returns (kind 0
+// CUBIC_SPLINE -- the engine's own choice --, 1 WENDLAND_C2, 2 GAUSSIAN; kernels.h:94-98)
+// (the loop bodies of compute_densities / compute_pressures / compute_forces,
+// src/sph_engine.cpp:203-244).  Writes rho[n], P[n], acc[3n].
+void ref_fields_k(int kind, size_t n, const float* pos, const float* vel, const float* mass,
+                  const float* params16, float* rho, float* P, float* acc) {
     const sph::SPHParameters prm = unpack_params(params16);
     sph::ParticleSystem ps(n > 0 ? n : 1);
     ps.add_particles(make_particles(n, pos, vel, mass));
-    auto kernel = sph::create_kernel(sph::KernelType::CUBIC_SPLINE, prm.smoothing_length);
+    auto kernel = sph::create_kernel(static_cast<sph::KernelType>(kind), prm.smoothing_length);
     sph::SpatialHash hash(prm.smoothing_length);
     hash.set_cell_size(prm.neighbor_search_radius);
     std::vector<glm::vec3> p = ps.get_positions();
@@ -148,6 +149,27 @@ void ref_fields(size_t n, const float* pos, const float* vel, const float* mass,
     for (size_t i = 0; i < n; ++i) {
         rho[i] = dens[i];
         P[i] = pres[i];
+    }
+}
+
+void ref_fields(size_t n, const float* pos, const float* vel, const float* mass,
+                const float* params16, float* rho, float* P, float* acc) {
+    ref_fields_k(0, n, pos, vel, mass, params16, rho, P, acc);
+}
+
+// W, gradW and laplacianW of create_kernel(kind, h) at n vectors r[3n]
+// (src/kernels.cpp:140-153, 172-200, 210-225).
+void ref_kernel_eval(int kind, float h, size_t n, const float* r, float* w, float* grad,
+                     float* lap) {
+    auto kernel = sph::create_kernel(static_cast<sph::KernelType>(kind), h);
+    for (size_t i = 0; i < n; ++i) {
+        const glm::vec3 v(r[3 * i], r[3 * i + 1], r[3 * i + 2]);
+        w[i] = kernel->W(v);
+        const glm::vec3 g = kernel->gradW(v);
+        grad[3 * i] = g.x;
+        grad[3 * i + 1] = g.y;
+        grad[3 * i + 2] = g.z;
+        lap[i] = kernel->laplacianW(v);
     }
 }
 

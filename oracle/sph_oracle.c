@@ -47,22 +47,34 @@ static inline uint64_t pack_cell(int32_t x, int32_t y, int32_t z) {
            ((uint64_t)((uint32_t)y & 0x1FFFFFu) << 21) | (uint64_t)((uint32_t)z & 0x1FFFFFu);
 }
 
-/* Cubic spline constants, computed in float exactly as CubicSplineKernel's constructor
- * (src/kernels.cpp:12-14, 23-36). */
+/* Smoothing kernels: the three of create_kernel (src/kernels.cpp:226-236), constants
+ * computed in float exactly as their constructors do (src/kernels.cpp:12-14, 23-36,
+ * 166-170, 204-208).  kind: 0 CUBIC_SPLINE, 1 WENDLAND_C2, 2 GAUSSIAN (KernelType order,
+ * src/kernels.h:94-98). */
 typedef struct {
-    float h, h_sq, sigma;
-} cubic;
+    int kind;
+    float h, h_sq, sigma;   /* cubic: sigma_3d_ */
+    float norm;             /* Wendland: norm_factor_; Gaussian: norm_ */
+    float s;                /* Gaussian: sigma_sq_inv_ */
+} kern;
 
-static cubic make_cubic(float h) {
-    cubic k;
+static kern make_kernel(int kind, float h) {
+    kern k;
+    memset(&k, 0, sizeof(k));
+    k.kind = kind;
     k.h = h;
     k.h_sq = h * h;
     k.sigma = 1.0f / ((((float)M_PI) * h) * h * h);
+    if (kind == 1) k.norm = 21.0f / (((2.0f * (float)M_PI) * h) * h * h);
+    if (kind == 2) {
+        k.s = 1.0f / (h * h);
+        k.norm = 1.0f / powf(((float)M_PI * h) * h, 1.5f);
+    }
     return k;
 }
 
-/* W_3d (src/kernels.cpp:58-66) */
-static inline float w3(const cubic* k, float q) {
+/* CubicSplineKernel::W_3d (src/kernels.cpp:58-66) */
+static inline float w3(const kern* k, float q) {
     if (q >= 0.0f && q <= 1.0f) {
         return k->sigma * (2.0f / 3.0f - q * q + 0.5f * q * q * q);
     } else if (q > 1.0f && q <= 2.0f) {
@@ -72,14 +84,49 @@ static inline float w3(const cubic* k, float q) {
     return 0.0f;
 }
 
-/* W(r) = W_3d(length(r)/h) (src/kernels.cpp:140-143, kernels.h:117-119) */
-static inline float w_of(const cubic* k, float rx, float ry, float rz) {
+/* Kernel::W(r): cubic W_3d(length(r)/h) (src/kernels.cpp:140-143, kernels.h:117-119);
+ * WendlandC2Kernel::W (kernels.cpp:172-178); GaussianKernel::W (kernels.cpp:210-213) */
+static inline float w_of(const kern* k, float rx, float ry, float rz) {
+    if (k->kind == 2) {
+        const float r_sq = dot3(rx, ry, rz);
+        return k->norm * expf(-r_sq * k->s);
+    }
     const float q = sqrtf(dot3(rx, ry, rz)) / k->h;
+    if (k->kind == 1) {
+        if (q >= 2.0f) return 0.0f;
+        const float tmp = 1.0f - 0.5f * q;
+        return k->norm * tmp * tmp * tmp * tmp * (2.0f * q + 1.0f);
+    }
     return w3(k, q);
 }
 
-/* gradW (src/kernels.cpp:96-108, 145-148) */
-static inline void gradw_of(const cubic* k, float rx, float ry, float rz, float* g) {
+/* Kernel::gradW(r): cubic (src/kernels.cpp:96-108, 145-148); Wendland (kernels.cpp:180-192);
+ * Gaussian (kernels.cpp:215-219) */
+static inline void gradw_of(const kern* k, float rx, float ry, float rz, float* g) {
+    if (k->kind == 2) {
+        const float r_sq = dot3(rx, ry, rz);
+        const float e = expf(-r_sq * k->s);
+        const float c = -2.0f * k->s * k->norm * e;
+        g[0] = c * rx;
+        g[1] = c * ry;
+        g[2] = c * rz;
+        return;
+    }
+    if (k->kind == 1) {
+        const float r_len = sqrtf(dot3(rx, ry, rz));
+        g[0] = g[1] = g[2] = 0.0f;
+        if (r_len < 1e-6f) return;
+        const float q = r_len / k->h;
+        if (q >= 2.0f) return;
+        const float tmp = 1.0f - 0.5f * q;
+        const float dw = -5.0f * tmp * tmp * tmp * q;
+        const float c = k->norm * dw;
+        const float den = r_len * k->h;
+        g[0] = c * (rx / den);
+        g[1] = c * (ry / den);
+        g[2] = c * (rz / den);
+        return;
+    }
     const float q = sqrtf(dot3(rx, ry, rz)) / k->h;
     const float r_len = sqrtf(dot3(rx, ry, rz));
     if (r_len < 1e-6f) {
@@ -104,9 +151,20 @@ static inline void gradw_of(const cubic* k, float rx, float ry, float rz, float*
     g[2] = gz / k->h;
 }
 
-/* laplacianW (src/kernels.cpp:130-138, 150-153) */
-static inline float lapw_of(const cubic* k, float rx, float ry, float rz) {
+/* Kernel::laplacianW(r): cubic (src/kernels.cpp:130-138, 150-153); Wendland
+ * (kernels.cpp:194-200); Gaussian (kernels.cpp:221-225) */
+static inline float lapw_of(const kern* k, float rx, float ry, float rz) {
+    if (k->kind == 2) {
+        const float r_sq = dot3(rx, ry, rz);
+        const float e = expf(-r_sq * k->s);
+        return 2.0f * k->s * k->norm * e * (2.0f * k->s * r_sq - 3.0f);
+    }
     const float q = sqrtf(dot3(rx, ry, rz)) / k->h;
+    if (k->kind == 1) {
+        if (q >= 2.0f) return 0.0f;
+        const float tmp = 1.0f - 0.5f * q;
+        return k->norm * (5.0f / k->h_sq) * tmp * tmp * (5.0f * q - 3.0f);
+    }
     if (q >= 0.0f && q <= 1.0f) {
         return k->sigma * (-2.0f + 3.0f * q) / k->h_sq;
     } else if (q > 1.0f && q <= 2.0f) {
@@ -280,7 +338,7 @@ int64_t orc_query(size_t n, const float* pos, float cell_size, float radius, int
 
 /* compute_densities -> equations::compute_density (src/sph_engine.cpp:203-212, 370-383) */
 static void densities(size_t n, const float* pos, const float* mass, const i64vec* nl,
-                      const cubic* k, float* rho) {
+                      const kern* k, float* rho) {
     const float w0 = w_of(k, 0.0f, 0.0f, 0.0f);
 #pragma omp parallel for schedule(static)
     for (long long i = 0; i < (long long)n; ++i) {
@@ -307,7 +365,7 @@ static void pressures(size_t n, const float* rho, float rest, float gas, float* 
 /* compute_forces: pressure force, viscosity force, external force, acceleration
  * (src/sph_engine.cpp:226-244, 390-443) */
 static void forces(size_t n, const float* pos, const float* vel, const float* mass,
-                   const i64vec* nl, const cubic* k, const float* rho, const float* P,
+                   const i64vec* nl, const kern* k, const float* rho, const float* P,
                    float viscosity, float gravity, float* acc) {
 #pragma omp parallel for schedule(static)
     for (long long i = 0; i < (long long)n; ++i) {
@@ -357,9 +415,14 @@ static void load_params(const float* p, float* out16) { memcpy(out16, p, 16 * si
 
 void orc_fields(size_t n, const float* pos, const float* vel, const float* mass,
                 const float* params16, float* rho, float* P, float* acc) {
+    orc_fields_k(0, n, pos, vel, mass, params16, rho, P, acc);
+}
+
+void orc_fields_k(int kind, size_t n, const float* pos, const float* vel, const float* mass,
+                  const float* params16, float* rho, float* P, float* acc) {
     float prm[16];
     load_params(params16, prm);
-    const cubic k = make_cubic(prm[3]);
+    const kern k = make_kernel(kind, prm[3]);
     i64vec* nl = (i64vec*)calloc(n ? n : 1, sizeof(i64vec));
     build_lists(n, pos, prm[15], prm[15], nl, NULL);
     densities(n, pos, mass, nl, &k, rho);
@@ -379,9 +442,49 @@ static inline double w3d(double sigma, double q) {
     return 0.0;
 }
 
+/* W, grad W = G * r and laplacian W of the three kernels in double (same formulas as the
+ * float versions above, evaluated in double) */
+static inline double w_d(int kind, double h, double sigma, double rl) {
+    const double q = rl / h;
+    if (kind == 1) {
+        if (q >= 2.0) return 0.0;
+        const double t = 1.0 - 0.5 * q;
+        return 21.0 / (2.0 * M_PI * h * h * h) * t * t * t * t * (2.0 * q + 1.0);
+    }
+    if (kind == 2) return exp(-rl * rl / (h * h)) / pow(M_PI * h * h, 1.5);
+    return w3d(sigma, q);
+}
+static inline double g_d(int kind, double h, double rl) {
+    const double q = rl / h;
+    if (kind == 1) {
+        if (q >= 2.0) return 0.0;
+        const double t = 1.0 - 0.5 * q;
+        return 21.0 / (2.0 * M_PI * h * h * h) * (-5.0 * t * t * t * q) / (rl * h);
+    }
+    /* kind 2 */
+    return -2.0 / (h * h) * exp(-rl * rl / (h * h)) / pow(M_PI * h * h, 1.5);
+}
+static inline double lap_d(int kind, double h, double rl) {
+    const double q = rl / h;
+    if (kind == 1) {
+        if (q >= 2.0) return 0.0;
+        const double t = 1.0 - 0.5 * q;
+        return 21.0 / (2.0 * M_PI * h * h * h) * (5.0 / (h * h)) * t * t * (5.0 * q - 3.0);
+    }
+    /* kind 2 */
+    const double s = 1.0 / (h * h);
+    return 2.0 * s * exp(-rl * rl * s) / pow(M_PI * h * h, 1.5) * (2.0 * s * rl * rl - 3.0);
+}
+
 void orc_fields_f64(size_t n, const float* pos, const float* vel, const float* mass,
                     const float* params16, double* rho, double* P, double* acc,
                     double* sum_abs) {
+    orc_fields_f64_k(0, n, pos, vel, mass, params16, rho, P, acc, sum_abs);
+}
+
+void orc_fields_f64_k(int kind, size_t n, const float* pos, const float* vel,
+                      const float* mass, const float* params16, double* rho, double* P,
+                      double* acc, double* sum_abs) {
     float prm[16];
     load_params(params16, prm);
     const double h = prm[3], hsq = h * h, sigma = 1.0 / (M_PI * h * h * h);
@@ -389,14 +492,14 @@ void orc_fields_f64(size_t n, const float* pos, const float* vel, const float* m
     build_lists(n, pos, prm[15], prm[15], nl, NULL);
 #pragma omp parallel for schedule(static)
     for (long long i = 0; i < (long long)n; ++i) {
-        double d = (double)mass[i] * w3d(sigma, 0.0);
+        double d = (double)mass[i] * w_d(kind, h, sigma, 0.0);
         for (size_t e = 0; e < nl[i].size; ++e) {
             const int64_t j = nl[i].data[e];
             if (j == i) continue;
             const double rx = (double)pos[3 * i] - (double)pos[3 * j];
             const double ry = (double)pos[3 * i + 1] - (double)pos[3 * j + 1];
             const double rz = (double)pos[3 * i + 2] - (double)pos[3 * j + 2];
-            d += (double)mass[j] * w3d(sigma, sqrt(rx * rx + ry * ry + rz * rz) / h);
+            d += (double)mass[j] * w_d(kind, h, sigma, sqrt(rx * rx + ry * ry + rz * rz));
         }
         rho[i] = d;
         P[i] = (double)prm[1] * (d - (double)prm[0]);
@@ -413,18 +516,28 @@ void orc_fields_f64(size_t n, const float* pos, const float* vel, const float* m
             const double rl = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
             const double q = rl / h;
             if (rl >= 1e-6) {
-                double c = 0.0;
-                if (q <= 1.0) c = sigma * (-2.0 * q + 1.5 * q * q);
-                else if (q <= 2.0) c = -sigma * 0.5 * (2.0 - q) * (2.0 - q);
                 const double s = (double)mass[j] * (P[i] + P[j]) / (2.0 * rho[j]);
-                for (int a = 0; a < 3; ++a) {
-                    const double t = s * c * (r[a] / rl) / h;
-                    f[a] -= t;
-                    sa[a] += fabs(t);
+                if (kind == 0) {
+                    double c = 0.0;
+                    if (q <= 1.0) c = sigma * (-2.0 * q + 1.5 * q * q);
+                    else if (q <= 2.0) c = -sigma * 0.5 * (2.0 - q) * (2.0 - q);
+                    for (int a = 0; a < 3; ++a) {
+                        const double t = s * c * (r[a] / rl) / h;
+                        f[a] -= t;
+                        sa[a] += fabs(t);
+                    }
+                } else {
+                    const double G = g_d(kind, h, rl);
+                    for (int a = 0; a < 3; ++a) {
+                        const double t = s * G * r[a];
+                        f[a] -= t;
+                        sa[a] += fabs(t);
+                    }
                 }
             }
             double lap = 0.0;
-            if (q <= 1.0) lap = sigma * (-2.0 + 3.0 * q) / hsq;
+            if (kind != 0) lap = lap_d(kind, h, rl);
+            else if (q <= 1.0) lap = sigma * (-2.0 + 3.0 * q) / hsq;
             else if (q <= 2.0) lap = sigma * (2.0 - q) / hsq;
             const double s = (double)mass[j] / rho[j] * (double)prm[2];
             for (int a = 0; a < 3; ++a) {
@@ -584,6 +697,7 @@ struct orc_engine {
     float prm[16];
     float cell_size;
     int initialized;
+    int kind; /* smoothing kernel (0 cubic spline, the reference engine's fixed choice) */
     float time, last_dt;
     uint64_t steps, max_nn, total_q;
 };
@@ -622,6 +736,8 @@ void orc_engine_free(orc_engine* e) {
 }
 
 /* SPHEngine::initialize (src/sph_engine.cpp:20-33) */
+void orc_engine_set_kernel(orc_engine* e, int kind) { e->kind = kind; }
+
 void orc_engine_initialize(orc_engine* e, const float* params16) {
     load_params(params16, e->prm);
     e->cell_size = e->prm[15];
@@ -676,7 +792,7 @@ void orc_engine_step(orc_engine* e, float dt) {
     build_lists(n, e->pos, e->cell_size, e->prm[15], e->nl, &mx);
     e->total_q += n;
     if (mx > e->max_nn) e->max_nn = mx;
-    const cubic k = make_cubic(e->prm[3]);
+    const kern k = make_kernel(e->kind, e->prm[3]);
     densities(n, e->pos, e->mass, e->nl, &k, e->rho);
     pressures(n, e->rho, e->prm[0], e->prm[1], e->P);
     forces(n, e->pos, e->vel, e->mass, e->nl, &k, e->rho, e->P, e->prm[2], e->prm[6], e->acc);

@@ -30,6 +30,12 @@ int64_t orc_query(size_t n, const float* pos, float cell_size, float radius, int
 void orc_fields(size_t n, const float* pos, const float* vel, const float* mass,
                 const float* params16, float* rho, float* P, float* acc);
 
+/* orc_fields with the smoothing kernel `kind` of create_kernel (src/kernels.cpp:226-236):
+ * 0 CUBIC_SPLINE, 1 WENDLAND_C2, 2 GAUSSIAN, evaluated through the equations:: formulas
+ * (the reference engine itself always uses the cubic spline, sph_engine.cpp:17, 23, 162). */
+void orc_fields_k(int kind, size_t n, const float* pos, const float* vel, const float* mass,
+                  const float* params16, float* rho, float* P, float* acc);
+
 /* The same evaluation in FP64 over the same (FP32-defined) neighbour sets: the
  * high-precision reference for error figures.  Optionally (sum_abs != NULL) also returns,
  * per particle and component, the sum of |term| of the acceleration's pair terms divided
@@ -37,6 +43,10 @@ void orc_fields(size_t n, const float* pos, const float* vel, const float* mass,
 void orc_fields_f64(size_t n, const float* pos, const float* vel, const float* mass,
                     const float* params16, double* rho, double* P, double* acc,
                     double* sum_abs);
+
+void orc_fields_f64_k(int kind, size_t n, const float* pos, const float* vel,
+                      const float* mass, const float* params16, double* rho, double* P,
+                      double* acc, double* sum_abs);
 
 /* FP64 evaluation on FP64 positions (the truth for the precision study): neighbour sets
  * by dot(x_i - x_j, x_i - x_j) <= r^2 in double, density/pressure/acceleration in double
@@ -49,6 +59,8 @@ typedef struct orc_engine orc_engine;
 orc_engine* orc_engine_new(size_t capacity);
 void orc_engine_free(orc_engine* e);
 void orc_engine_initialize(orc_engine* e, const float* params16);
+/* Smoothing kernel of the engine's step (kind as in orc_fields_k; default 0). */
+void orc_engine_set_kernel(orc_engine* e, int kind);
 /* Appends particles; beyond capacity they are dropped (src/particle.cpp:26-33).
  * vel may be NULL (zero velocity). */
 void orc_engine_add(orc_engine* e, size_t n, const float* pos, const float* vel,

@@ -45,6 +45,9 @@ class _Lib:
         f = getattr(L, f"{pf}_fields")
         f.restype = None
         f.argtypes = [C.c_size_t] + [C.c_void_p] * 7
+        fk = getattr(L, f"{pf}_fields_k")
+        fk.restype = None
+        fk.argtypes = [C.c_int, C.c_size_t] + [C.c_void_p] * 7
         e = f"{pf}_engine_"
         getattr(L, e + "new").restype = C.c_void_p
         getattr(L, e + "new").argtypes = [C.c_size_t]
@@ -71,8 +74,9 @@ class _Lib:
         fn(n, _p(pos), C.c_float(cs), C.c_float(radius), _p(counts), _p(idx))
         return counts, idx[:total]
 
-    def fields(self, pos, vel, mass, params16):
-        """rho, P, acc of one evaluation of the step's field phases."""
+    def fields(self, pos, vel, mass, params16, kernel: int = 0):
+        """rho, P, acc of one evaluation of the step's field phases with the smoothing
+        kernel `kernel` (0 cubic spline, 1 Wendland C2, 2 Gaussian)."""
         pos = _f32(pos).reshape(-1, 3)
         n = pos.shape[0]
         vel = _f32(vel).reshape(n, 3)
@@ -81,8 +85,8 @@ class _Lib:
         rho = np.zeros(n, np.float32)
         P = np.zeros(n, np.float32)
         acc = np.zeros((n, 3), np.float32)
-        getattr(self.lib, f"{self.prefix}_fields")(n, _p(pos), _p(vel), _p(mass), _p(prm),
-                                                    _p(rho), _p(P), _p(acc))
+        getattr(self.lib, f"{self.prefix}_fields_k")(int(kernel), n, _p(pos), _p(vel), _p(mass),
+                                                      _p(prm), _p(rho), _p(P), _p(acc))
         return rho, P, acc
 
 
@@ -93,6 +97,8 @@ class Port(_Lib):
         super().__init__(path)
         L = self.lib
         L.orc_fields_f64.argtypes = [C.c_size_t] + [C.c_void_p] * 8
+        L.orc_fields_f64_k.argtypes = [C.c_int, C.c_size_t] + [C.c_void_p] * 8
+        L.orc_engine_set_kernel.argtypes = [C.c_void_p, C.c_int]
         L.orc_fields_f64d.argtypes = [C.c_size_t] + [C.c_void_p] * 7
         L.orc_fields_f64d.restype = C.c_int64
         L.orc_engine_get.argtypes = [C.c_void_p] + [C.c_void_p] * 5
@@ -104,7 +110,7 @@ class Port(_Lib):
         L.orc_max_threads.restype = C.c_int
         L.orc_set_threads.argtypes = [C.c_int]
 
-    def fields_f64(self, pos, vel, mass, params16, want_scale: bool = False):
+    def fields_f64(self, pos, vel, mass, params16, want_scale: bool = False, kernel: int = 0):
         pos = _f32(pos).reshape(-1, 3)
         n = pos.shape[0]
         vel = _f32(vel).reshape(n, 3)
@@ -114,8 +120,8 @@ class Port(_Lib):
         P = np.zeros(n)
         acc = np.zeros((n, 3))
         scale = np.zeros((n, 3)) if want_scale else None
-        self.lib.orc_fields_f64(n, _p(pos), _p(vel), _p(mass), _p(prm), _p(rho), _p(P),
-                                _p(acc), _p(scale))
+        self.lib.orc_fields_f64_k(int(kernel), n, _p(pos), _p(vel), _p(mass), _p(prm), _p(rho),
+                                  _p(P), _p(acc), _p(scale))
         return (rho, P, acc, scale) if want_scale else (rho, P, acc)
 
     def fields_f64d(self, pos64, vel, mass, params16):
@@ -201,6 +207,12 @@ class Engine:
                         rho_cap=rho, pressure_cap=P)
         self.o.lib.ref_engine_get(self.h, _p(pos), _p(vel), _p(rho), _p(P))
         return dict(pos=pos, vel=vel, rho=rho[:n], pressure=P[:n], rho_cap=rho, pressure_cap=P)
+
+    def set_kernel(self, kind: int):
+        """Smoothing kernel of the oracle engine's step (0 cubic spline, 1 Wendland C2,
+        2 Gaussian)."""
+        assert isinstance(self.o, Port)
+        self.o.lib.orc_engine_set_kernel(self.h, int(kind))
 
     def set_state(self, pos, vel):
         assert isinstance(self.o, Port)

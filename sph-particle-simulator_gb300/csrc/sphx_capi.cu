@@ -25,6 +25,7 @@ struct sphx_ctx {
     bool have_fields = false;  // rho/P/acc of the current particle set exist
     StepConst sc{};
     Buffers b{};
+    int kernel = SPHX_KERNEL_CUBIC_SPLINE;
     DevState* ds = nullptr;
     float* stage = nullptr;    // 10 * capacity floats (room for FP64 positions)
     float4* snap_pos = nullptr;
@@ -146,6 +147,23 @@ void fill_step_const_from(sphx_ctx* c, const sphx_params& p, size_t n, StepConst
     // W(vec3(0)): q = length(0) / h
     const float q0 = std::sqrt(0.0f) / h;
     s.w0 = host_cubic_w(s.sigma, q0);
+    s.kern = c->kernel;
+    s.wnorm = s.wl = s.gs = s.gg = s.gl = s.g2s = 0.0f;
+    if (c->kernel == SPHX_KERNEL_WENDLAND_C2) {
+        // WendlandC2Kernel(h) (kernels.cpp:166-170); W(0) as WendlandC2Kernel::W computes it
+        s.wnorm = 21.0f / (2.0f * static_cast<float>(M_PI) * h * h * h);
+        s.wl = s.wnorm * (5.0f / s.h_sq);
+        const float tmp = 1.0f - 0.5f * q0;
+        s.w0 = s.wnorm * tmp * tmp * tmp * tmp * (2.0f * q0 + 1.0f);
+    } else if (c->kernel == SPHX_KERNEL_GAUSSIAN) {
+        // GaussianKernel(h) (kernels.cpp:203-208); W(0) = norm_ * exp(-0 * sigma_sq_inv_)
+        s.gs = 1.0f / (h * h);
+        s.wnorm = 1.0f / std::pow(static_cast<float>(M_PI) * h * h, 1.5f);
+        s.gg = -2.0f * s.gs * s.wnorm;
+        s.gl = 2.0f * s.gs * s.wnorm;
+        s.g2s = 2.0f * s.gs;
+        s.w0 = s.wnorm * std::exp(-0.0f * s.gs);
+    }
     s.rest = p.rest_density;
     s.gas = p.gas_constant;
     s.visc = p.viscosity;
@@ -472,6 +490,36 @@ int sphx_set_params(sphx_ctx* c, const sphx_params* p) {
     c->params = *p;
     c->have_params = true;
     c->version++;
+    return SPHX_OK;
+}
+
+int sphx_set_kernel(sphx_ctx* c, int kernel) {
+    int rc = enter(c);
+    if (rc) return rc;
+    if (kernel != SPHX_KERNEL_CUBIC_SPLINE && kernel != SPHX_KERNEL_WENDLAND_C2 &&
+        kernel != SPHX_KERNEL_GAUSSIAN)
+        return SPHX_ERR_INVALID_ARG;
+    if (kernel != c->kernel) {
+        c->kernel = kernel;
+        if (c->nscenes) {  // refresh the scenes' constants, keep their state
+            SPHX_CUDA(cudaStreamSynchronize(c->stream));
+            std::vector<SceneInfo> info(c->nscenes);
+            SPHX_CUDA(cudaMemcpy(info.data(), c->b.scenes, c->nscenes * sizeof(SceneInfo),
+                                 cudaMemcpyDeviceToHost));
+            for (uint32_t s = 0; s < c->nscenes; ++s)
+                fill_step_const_from(c, c->scene_params[s], info[s].count, info[s].c);
+            SPHX_CUDA(cudaMemcpy(c->b.scenes, info.data(), c->nscenes * sizeof(SceneInfo),
+                                 cudaMemcpyHostToDevice));
+        }
+        c->have_fields = false;
+        c->version++;
+    }
+    return SPHX_OK;
+}
+
+int sphx_get_kernel(sphx_ctx* c, int* kernel) {
+    if (!c || !kernel) return SPHX_ERR_INVALID_ARG;
+    *kernel = c->kernel;
     return SPHX_OK;
 }
 

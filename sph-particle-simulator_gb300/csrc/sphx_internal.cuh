@@ -44,6 +44,14 @@ struct StepConst {
     // division by the fixed divisors h and h*h (see xdiv_fixed)
     float rcp_h, rcp_hsq;  // RN(1/h), RN(1/h^2)
     int fast_div_h, fast_div_hsq;  // 1: the one-correction sequence is verified for it
+    // smoothing kernel (SPHX_KERNEL_*) and the constants its constructor computes in float
+    int kern;
+    float wnorm;  // Wendland norm_factor_ 21/(2 pi h^3); Gaussian norm_ 1/(pi h^2)^1.5
+    float wl;     // Wendland norm_factor_ * (5 / h_sq)
+    float gs;     // Gaussian sigma_sq_inv_ = 1 / (h h)
+    float gg;     // Gaussian -2 sigma_sq_inv_ norm_
+    float gl;     // Gaussian 2 sigma_sq_inv_ norm_
+    float g2s;    // Gaussian 2 sigma_sq_inv_
 };
 
 // Device-resident scalars written and read by the kernels of a step.
@@ -199,6 +207,22 @@ __device__ __forceinline__ float cubic_lap(const StepConst& c, float q) {
         return xdiv_fixed(xmul(c.sigma, tmp), c.h_sq, c.rcp_hsq, c.fast_div_hsq);
     }
     return 0.0f;
+}
+
+// WendlandC2Kernel::W after q = length(r)/h (kernels.cpp:172-178):
+// norm * tmp^4 * (2q + 1), tmp = 1 - q/2, 0 for q >= 2
+__device__ __forceinline__ float wendland_w(const StepConst& c, float q) {
+    if (q >= 2.0f) return 0.0f;
+    const float tmp = xsub(1.0f, xmul(0.5f, q));
+    return xmul(xmul(xmul(xmul(xmul(c.wnorm, tmp), tmp), tmp), tmp), xadd(xmul(2.0f, q), 1.0f));
+}
+
+// WendlandC2Kernel::laplacianW after q (kernels.cpp:194-200):
+// norm * (5 / h_sq) * tmp * tmp * (5q - 3), 0 for q >= 2
+__device__ __forceinline__ float wendland_lap(const StepConst& c, float q) {
+    if (q >= 2.0f) return 0.0f;
+    const float tmp = xsub(1.0f, xmul(0.5f, q));
+    return xmul(xmul(xmul(c.wl, tmp), tmp), xsub(xmul(5.0f, q), 3.0f));
 }
 
 __device__ __forceinline__ bool finite3(float x, float y, float z) {

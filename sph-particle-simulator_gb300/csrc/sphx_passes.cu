@@ -357,6 +357,27 @@ __device__ __forceinline__ float cubic_w_p(const StepConst& c, float q) {
     return 0.0f;
 }
 
+// W of the pair (x_i - x_j = (dx, dy, dz), d2 = |.|^2) for smoothing kernel K.
+// Exact mode: the reference's float operations (Kernel::W, kernels.cpp:140-143, 172-178,
+// 210-213); precision mode: contracted arithmetic.
+template <int K>
+__device__ __forceinline__ float pair_w_exact(const StepConst& c, float d2) {
+    if (K == SPHX_KERNEL_GAUSSIAN) return xmul(c.wnorm, expf(xmul(-d2, c.gs)));
+    const float q = xdiv_fixed(xsqrt(d2), c.h, c.rcp_h, c.fast_div_h);
+    return K == SPHX_KERNEL_WENDLAND_C2 ? wendland_w(c, q) : cubic_w(c, q);
+}
+template <int K>
+__device__ __forceinline__ float pair_w_p(const StepConst& c, float d2) {
+    if (K == SPHX_KERNEL_GAUSSIAN) return c.wnorm * expf(-d2 * c.gs);
+    const float q = sqrtf(d2) / c.h;
+    if (K == SPHX_KERNEL_WENDLAND_C2) {
+        if (q >= 2.0f) return 0.0f;
+        const float t = 1.0f - 0.5f * q;
+        return c.wnorm * (t * t) * (t * t) * (2.0f * q + 1.0f);
+    }
+    return cubic_w_p(c, q);
+}
+
 // Work distribution: warps take tiles from a per-pass counter (dynamic, so crowded cells
 // in degenerate states do not serialise the tail).
 __device__ __forceinline__ uint32_t next_tile(uint32_t* ctr, int lane) {
@@ -380,7 +401,7 @@ struct DensitySmem {
     float tbuf[kDensityBatch];
 };
 
-template <bool kPrecise, bool kBatch>
+template <bool kPrecise, bool kBatch, int kKern>
 __global__ void __launch_bounds__(128, 8) k_density(const StepConst cp, const Buffers b,
                                                  DevState* ds) {
     if (ds->status) return;
@@ -474,12 +495,10 @@ __global__ void __launch_bounds__(128, 8) k_density(const StepConst cp, const Bu
                         if (kPrecise) {
                             const float4 xt = S->tpos[pr >> 5];
                             const float dx = xt.x - xj.x, dy = xt.y - xj.y, dz = xt.z - xj.z;
-                            const float q = sqrtf(dx * dx + dy * dy + dz * dz) / c.h;
-                            S->tbuf[f - base] = xj.w * cubic_w_p(c, q);
+                            S->tbuf[f - base] = xj.w * pair_w_p<kKern>(c, dx * dx + dy * dy + dz * dz);
                         } else {
                             const Diff d = diff(S->tpos[pr >> 5], xj);
-                            const float q = xdiv_fixed(xsqrt(d.d2), c.h, c.rcp_h, c.fast_div_h);
-                            S->tbuf[f - base] = xmul(xj.w, cubic_w(c, q));
+                            S->tbuf[f - base] = xmul(xj.w, pair_w_exact<kKern>(c, d.d2));
                         }
                     }
                     __syncwarp();
@@ -532,30 +551,65 @@ struct ForceSmem {
 // where the reference skips it: subtracting +0 leaves every float unchanged) and the
 // viscosity contribution ((m_j/rho_j) mu (v_j - v_t)) laplacianW (added), each with the
 // reference's operations.
+template <int K>
 __device__ __forceinline__ void force_term(const StepConst& c, const float4& xt,
                                            const float4& vt, float Pt, const float4& xj,
                                            const float4& vj, const float4& aj, float* p3,
                                            float* v3) {
     const Diff d = diff(xt, xj);
     const float r_len = xsqrt(d.d2);
-    const float q = xdiv_fixed(r_len, c.h, c.rcp_h, c.fast_div_h);
     const bool skip = r_len < 1e-6f;
     p3[0] = p3[1] = p3[2] = 0.0f;
-    if (!skip) {
-        const float pt = xdiv(xadd(Pt, aj.y), aj.z);
-        float gx = 0.0f, gy = 0.0f, gz = 0.0f;
-        if ((q >= 0.0f && q <= 1.0f) || (q > 1.0f && q <= 2.0f)) {
-            const float gf = cubic_grad_factor(c, q);
-            gx = xmul(gf, xdiv(d.x, r_len));
-            gy = xmul(gf, xdiv(d.y, r_len));
-            gz = xmul(gf, xdiv(d.z, r_len));
+    float lap;
+    if (K == SPHX_KERNEL_GAUSSIAN) {
+        // GaussianKernel::gradW / laplacianW (kernels.cpp:215-225): both use
+        // exp(-r_sq * sigma_sq_inv_) of the same r_sq -- one evaluation serves both
+        const float e = expf(xmul(-d.d2, c.gs));
+        if (!skip) {
+            const float pt = xdiv(xadd(Pt, aj.y), aj.z);
+            const float k = xmul(c.gg, e);
+            const float sp = xmul(xj.w, pt);
+            p3[0] = xmul(sp, xmul(k, d.x));
+            p3[1] = xmul(sp, xmul(k, d.y));
+            p3[2] = xmul(sp, xmul(k, d.z));
         }
-        const float sp = xmul(xj.w, pt);
-        p3[0] = xmul(sp, xdiv_fixed(gx, c.h, c.rcp_h, c.fast_div_h));
-        p3[1] = xmul(sp, xdiv_fixed(gy, c.h, c.rcp_h, c.fast_div_h));
-        p3[2] = xmul(sp, xdiv_fixed(gz, c.h, c.rcp_h, c.fast_div_h));
+        lap = xmul(xmul(c.gl, e), xsub(xmul(c.g2s, d.d2), 3.0f));
+    } else {
+        const float q = xdiv_fixed(r_len, c.h, c.rcp_h, c.fast_div_h);
+        if (!skip) {
+            const float pt = xdiv(xadd(Pt, aj.y), aj.z);
+            const float sp = xmul(xj.w, pt);
+            if (K == SPHX_KERNEL_WENDLAND_C2) {
+                // WendlandC2Kernel::gradW (kernels.cpp:180-192):
+                // norm * dW/dq * (r / (r_len h)), dW/dq = -5 tmp^3 q; 0 for q >= 2
+                if (!(q >= 2.0f)) {
+                    const float tmp = xsub(1.0f, xmul(0.5f, q));
+                    const float dw = xmul(xmul(xmul(xmul(-5.0f, tmp), tmp), tmp), q);
+                    const float gsc = xmul(c.wnorm, dw);
+                    const float den = xmul(r_len, c.h);
+                    p3[0] = xmul(sp, xmul(gsc, xdiv(d.x, den)));
+                    p3[1] = xmul(sp, xmul(gsc, xdiv(d.y, den)));
+                    p3[2] = xmul(sp, xmul(gsc, xdiv(d.z, den)));
+                } else {
+                    p3[0] = xmul(sp, 0.0f);
+                    p3[1] = xmul(sp, 0.0f);
+                    p3[2] = xmul(sp, 0.0f);
+                }
+            } else {
+                float gx = 0.0f, gy = 0.0f, gz = 0.0f;
+                if ((q >= 0.0f && q <= 1.0f) || (q > 1.0f && q <= 2.0f)) {
+                    const float gf = cubic_grad_factor(c, q);
+                    gx = xmul(gf, xdiv(d.x, r_len));
+                    gy = xmul(gf, xdiv(d.y, r_len));
+                    gz = xmul(gf, xdiv(d.z, r_len));
+                }
+                p3[0] = xmul(sp, xdiv_fixed(gx, c.h, c.rcp_h, c.fast_div_h));
+                p3[1] = xmul(sp, xdiv_fixed(gy, c.h, c.rcp_h, c.fast_div_h));
+                p3[2] = xmul(sp, xdiv_fixed(gz, c.h, c.rcp_h, c.fast_div_h));
+            }
+        }
+        lap = K == SPHX_KERNEL_WENDLAND_C2 ? wendland_lap(c, q) : cubic_lap(c, q);
     }
-    const float lap = cubic_lap(c, q);
     const float sv = xmul(aj.w, c.visc);
     v3[0] = xmul(xmul(sv, xsub(vj.x, vt.x)), lap);
     v3[1] = xmul(xmul(sv, xsub(vj.y, vt.y)), lap);
@@ -563,27 +617,42 @@ __device__ __forceinline__ void force_term(const StepConst& c, const float4& xt,
 }
 
 // Precision-mode pair term: the same formulas with contracted FP32 arithmetic.
+template <int K>
 __device__ __forceinline__ void force_term_p(const StepConst& c, const float4& xt,
                                              const float4& vt, float Pt, const float4& xj,
                                              const float4& vj, const float4& aj, float* p3,
                                              float* v3) {
     const float dx = xt.x - xj.x, dy = xt.y - xj.y, dz = xt.z - xj.z;
-    const float r_len = sqrtf(dx * dx + dy * dy + dz * dz);
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    const float r_len = sqrtf(d2);
     const float q = r_len / c.h;
     const bool skip = r_len < 1e-6f;
     p3[0] = p3[1] = p3[2] = 0.0f;
-    if (!skip) {
+    float g = 0.0f, lap = 0.0f;  // grad W = g * r
+    if (K == SPHX_KERNEL_GAUSSIAN) {
+        const float e = expf(-d2 * c.gs);
+        g = c.gg * e;
+        lap = c.gl * e * (c.g2s * d2 - 3.0f);
+    } else if (K == SPHX_KERNEL_WENDLAND_C2) {
+        if (q < 2.0f) {
+            const float t = 1.0f - 0.5f * q;
+            g = c.wnorm * (-5.0f * t * t * t * q) / (r_len * c.h);
+            lap = c.wl * t * t * (5.0f * q - 3.0f);
+        }
+    } else {
         float gf = 0.0f;
         if (q <= 1.0f) gf = c.sigma * (-2.0f * q + 1.5f * q * q);
         else if (q <= 2.0f) gf = -c.sigma * 0.5f * (2.0f - q) * (2.0f - q);
-        const float s = xj.w * (Pt + aj.y) / aj.z * gf / (r_len * c.h);
+        g = gf / (r_len * c.h);
+        if (q <= 1.0f) lap = c.sigma * (-2.0f + 3.0f * q) / c.h_sq;
+        else if (q <= 2.0f) lap = c.sigma * (2.0f - q) / c.h_sq;
+    }
+    if (!skip) {
+        const float s = xj.w * (Pt + aj.y) / aj.z * g;
         p3[0] = s * dx;
         p3[1] = s * dy;
         p3[2] = s * dz;
     }
-    float lap = 0.0f;
-    if (q <= 1.0f) lap = c.sigma * (-2.0f + 3.0f * q) / c.h_sq;
-    else if (q <= 2.0f) lap = c.sigma * (2.0f - q) / c.h_sq;
     const float sv = aj.w * c.visc * lap;
     v3[0] = sv * (vj.x - vt.x);
     v3[1] = sv * (vj.y - vt.y);
@@ -630,7 +699,7 @@ __device__ __forceinline__ void integrate_cells(const StepConst& c, float dt, co
     }
 }
 
-template <bool kIntegrate, bool kPrecise, bool kBatch>
+template <bool kIntegrate, bool kPrecise, bool kBatch, int kKern>
 __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buffers b,
                                                DevState* ds) {
     if (ds->status) return;
@@ -726,11 +795,11 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buff
                         const int tt = pr >> 5, jj = pr & 31;
                         float p3[3], v3[3];
                         if (kPrecise)
-                            force_term_p(c, S->tpos[tt], S->tvel[tt], S->tP[tt], S->cpos[jj],
-                                         S->cvel[jj], S->caux[jj], p3, v3);
+                            force_term_p<kKern>(c, S->tpos[tt], S->tvel[tt], S->tP[tt],
+                                                S->cpos[jj], S->cvel[jj], S->caux[jj], p3, v3);
                         else
-                            force_term(c, S->tpos[tt], S->tvel[tt], S->tP[tt], S->cpos[jj],
-                                       S->cvel[jj], S->caux[jj], p3, v3);
+                            force_term<kKern>(c, S->tpos[tt], S->tvel[tt], S->tP[tt],
+                                              S->cpos[jj], S->cvel[jj], S->caux[jj], p3, v3);
                         const uint32_t u = f - base;
                         S->tbA[u] = make_float4(p3[0], p3[1], p3[2], v3[0]);
                         S->tbB[u] = make_float2(v3[1], v3[2]);
@@ -899,47 +968,66 @@ static int pass_blocks(const LaunchCtx& L) {
     return L.num_sms * bps;
 }
 
-template <bool kPrecise, bool kBatch>
+template <bool kPrecise, bool kBatch, int kKern>
 static void launch_density_t(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                              DevState* ds) {
     const int threads = 32 * L.warps_per_block;
     const size_t sm = (size_t)L.warps_per_block * sizeof(DensitySmem);
     static int blocks[5][8] = {};
     int& nb = blocks[L.warps_per_block][L.blocks_per_sm & 7];
-    if (!nb) nb = resident_blocks(L, k_density<kPrecise, kBatch>, threads, sm);
-    k_density<kPrecise, kBatch><<<nb, threads, sm, L.stream>>>(c, b, ds);
+    if (!nb) nb = resident_blocks(L, k_density<kPrecise, kBatch, kKern>, threads, sm);
+    k_density<kPrecise, kBatch, kKern><<<nb, threads, sm, L.stream>>>(c, b, ds);
+}
+
+template <int kKern>
+static void launch_density_k(const LaunchCtx& L, const StepConst& c, const Buffers& b,
+                             DevState* ds) {
+    if (b.nscenes > 0) launch_density_t<false, true, kKern>(L, c, b, ds);
+    else if (c.precise) launch_density_t<true, false, kKern>(L, c, b, ds);
+    else launch_density_t<false, false, kKern>(L, c, b, ds);
 }
 
 int launch_density(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds) {
-    if (b.nscenes > 0) launch_density_t<false, true>(L, c, b, ds);
-    else if (c.precise) launch_density_t<true, false>(L, c, b, ds);
-    else launch_density_t<false, false>(L, c, b, ds);
+    if (c.kern == SPHX_KERNEL_WENDLAND_C2) launch_density_k<SPHX_KERNEL_WENDLAND_C2>(L, c, b, ds);
+    else if (c.kern == SPHX_KERNEL_GAUSSIAN) launch_density_k<SPHX_KERNEL_GAUSSIAN>(L, c, b, ds);
+    else launch_density_k<SPHX_KERNEL_CUBIC_SPLINE>(L, c, b, ds);
     return 1;
 }
 
-template <bool kIntegrate, bool kPrecise, bool kBatch>
+template <bool kIntegrate, bool kPrecise, bool kBatch, int kKern>
 static void launch_force_t(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                            DevState* ds) {
     const int threads = 32 * L.warps_per_block;
     const size_t sm = (size_t)L.warps_per_block * sizeof(ForceSmem);
     static int blocks[5][8] = {};
     int& nb = blocks[L.warps_per_block][L.blocks_per_sm & 7];
-    if (!nb) nb = resident_blocks(L, k_force<kIntegrate, kPrecise, kBatch>, threads, sm);
-    k_force<kIntegrate, kPrecise, kBatch><<<nb, threads, sm, L.stream>>>(c, b, ds);
+    if (!nb) nb = resident_blocks(L, k_force<kIntegrate, kPrecise, kBatch, kKern>, threads, sm);
+    k_force<kIntegrate, kPrecise, kBatch, kKern><<<nb, threads, sm, L.stream>>>(c, b, ds);
+}
+
+template <int kKern>
+static void launch_force_k(const LaunchCtx& L, const StepConst& c, const Buffers& b,
+                           DevState* ds, int integrate) {
+    if (b.nscenes > 0) {
+        if (integrate) launch_force_t<true, false, true, kKern>(L, c, b, ds);
+        else launch_force_t<false, false, true, kKern>(L, c, b, ds);
+    } else if (integrate) {
+        if (c.precise) launch_force_t<true, true, false, kKern>(L, c, b, ds);
+        else launch_force_t<true, false, false, kKern>(L, c, b, ds);
+    } else {
+        if (c.precise) launch_force_t<false, true, false, kKern>(L, c, b, ds);
+        else launch_force_t<false, false, false, kKern>(L, c, b, ds);
+    }
 }
 
 int launch_force(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds,
                  int integrate) {
-    if (b.nscenes > 0) {
-        if (integrate) launch_force_t<true, false, true>(L, c, b, ds);
-        else launch_force_t<false, false, true>(L, c, b, ds);
-    } else if (integrate) {
-        if (c.precise) launch_force_t<true, true, false>(L, c, b, ds);
-        else launch_force_t<true, false, false>(L, c, b, ds);
-    } else {
-        if (c.precise) launch_force_t<false, true, false>(L, c, b, ds);
-        else launch_force_t<false, false, false>(L, c, b, ds);
-    }
+    if (c.kern == SPHX_KERNEL_WENDLAND_C2)
+        launch_force_k<SPHX_KERNEL_WENDLAND_C2>(L, c, b, ds, integrate);
+    else if (c.kern == SPHX_KERNEL_GAUSSIAN)
+        launch_force_k<SPHX_KERNEL_GAUSSIAN>(L, c, b, ds, integrate);
+    else
+        launch_force_k<SPHX_KERNEL_CUBIC_SPLINE>(L, c, b, ds, integrate);
     return 1;
 }
 

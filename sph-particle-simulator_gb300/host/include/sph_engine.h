@@ -14,8 +14,13 @@
 //    integration phase is fused into the force pass, so integration_time stays 0.
 //    max_neighbors / total_neighbor_queries are exact (the reference's are updated
 //    without synchronisation inside an OpenMP loop, sph_engine.cpp:350-351).
-//  * The kernel-function classes and equations:: free functions are not provided: the
-//    per-pair equations run only inside step(), on the GPU.
+//  * The kernel classes and create_kernel are provided (kernels.h) for user code; the
+//    equations:: free functions are not: the per-pair equations run only inside step(),
+//    on the GPU.
+//  * set_kernel_type / get_kernel_type (new) select the smoothing kernel of the step among
+//    the three create_kernel offers.  The reference engine always uses the cubic spline
+//    (sph_engine.cpp:17, 23, 162), which stays the default; the choice survives
+//    set_smoothing_length and initialize.
 //  * Device failures surface as std::runtime_error (the reference has none to report).
 #pragma once
 
@@ -23,6 +28,7 @@
 #include <memory>
 #include <vector>
 
+#include "kernels.h"
 #include "particle.h"
 #include "spatial_hash.h"
 
@@ -91,6 +97,10 @@ class SPHEngine {
     void set_smoothing_length(float h);
     void set_boundaries(float xmin, float xmax, float ymin, float ymax, float zmin, float zmax);
 
+    // Smoothing kernel of step() (an addition to the reference's API, see above).
+    void set_kernel_type(KernelType type);
+    KernelType get_kernel_type() const { return kernel_type_; }
+
     const PerformanceStats& get_performance_stats() const;
     void reset_performance_stats();
 
@@ -118,6 +128,7 @@ class SPHEngine {
 
     mutable ParticleSystem particles_;
     SPHParameters params_;
+    KernelType kernel_type_ = KernelType::CUBIC_SPLINE;
     sphx_ctx* gpu_ = nullptr;
     size_t step_count_ = 0;
     bool initialized_ = false;

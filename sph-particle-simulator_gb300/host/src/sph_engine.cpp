@@ -200,6 +200,14 @@ void SPHEngine::set_smoothing_length(float h) {
     push_params();
 }
 
+void SPHEngine::set_kernel_type(KernelType type) {
+    const int k = static_cast<int>(type);
+    if (k < SPHX_KERNEL_CUBIC_SPLINE || k > SPHX_KERNEL_GAUSSIAN)
+        throw std::invalid_argument("Unknown kernel type");
+    check(sphx_set_kernel(gpu_, k), "sphx_set_kernel");
+    kernel_type_ = type;
+}
+
 void SPHEngine::set_boundaries(float xmin, float xmax, float ymin, float ymax, float zmin,
                                float zmax) {
     params_.bounds.xmin = xmin;

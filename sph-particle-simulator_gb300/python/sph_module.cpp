@@ -104,6 +104,22 @@ PYBIND11_MODULE(sph, m) {
         .value("BOUNDARY", sph::ParticleType::BOUNDARY)
         .value("SOLID", sph::ParticleType::SOLID);
 
+    // smoothing kernels (kernels.h; the reference's module does not bind them)
+    py::enum_<sph::KernelType>(m, "KernelType")
+        .value("CUBIC_SPLINE", sph::KernelType::CUBIC_SPLINE)
+        .value("WENDLAND_C2", sph::KernelType::WENDLAND_C2)
+        .value("GAUSSIAN", sph::KernelType::GAUSSIAN);
+
+    py::class_<sph::Kernel>(m, "Kernel")
+        .def("W", &sph::Kernel::W)
+        .def("gradW", &sph::Kernel::gradW)
+        .def("laplacianW", &sph::Kernel::laplacianW)
+        .def("get_smoothing_length", &sph::Kernel::get_smoothing_length)
+        .def("set_smoothing_length", &sph::Kernel::set_smoothing_length)
+        .def("get_support_radius", &sph::Kernel::get_support_radius);
+
+    m.def("create_kernel", &sph::create_kernel, py::arg("type"), py::arg("smoothing_length"));
+
     py::class_<sph::Particle>(m, "Particle")
         .def(py::init<>())
         .def(py::init<const glm::vec3&, float, sph::ParticleType>(), py::arg("position"),
@@ -187,6 +203,8 @@ PYBIND11_MODULE(sph, m) {
         .def("set_viscosity", &sph::SPHEngine::set_viscosity)
         .def("set_smoothing_length", &sph::SPHEngine::set_smoothing_length)
         .def("set_boundaries", &sph::SPHEngine::set_boundaries)
+        .def("set_kernel_type", &sph::SPHEngine::set_kernel_type)
+        .def("get_kernel_type", &sph::SPHEngine::get_kernel_type)
         .def("get_performance_stats", &sph::SPHEngine::get_performance_stats,
              py::return_value_policy::copy)
         .def("reset_performance_stats", &sph::SPHEngine::reset_performance_stats)

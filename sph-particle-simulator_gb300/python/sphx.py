@@ -25,6 +25,10 @@ ERRORS = {
 MODE_EXACT = 0
 MODE_PRECISE = 1
 MODE_PRECISE_FP16 = 2
+# smoothing kernels (sph::KernelType order)
+KERNEL_CUBIC_SPLINE = 0
+KERNEL_WENDLAND_C2 = 1
+KERNEL_GAUSSIAN = 2
 
 # every symbol include/sphx.h declares
 EXPORTS = (
@@ -35,7 +39,7 @@ EXPORTS = (
     "sphx_snapshot", "sphx_restore", "sphx_debug_pairs", "sphx_grid_create",
     "sphx_grid_destroy", "sphx_grid_build", "sphx_grid_query", "sphx_grid_info",
     "sphx_grid_cell", "sphx_set_scenes", "sphx_get_scene_stats", "sphx_autotune",
-    "sphx_density_noalloc",
+    "sphx_density_noalloc", "sphx_set_kernel", "sphx_get_kernel",
 )
 NOALLOC_MAX_PARTICLES = 65536
 
@@ -100,6 +104,8 @@ def load_library(path: Path | str = LIB_PATH) -> C.CDLL:
         "sphx_destroy": ([vp], None),
         "sphx_set_stream": ([vp, vp], C.c_int),
         "sphx_set_params": ([vp, C.POINTER(SphxParams)], C.c_int),
+        "sphx_set_kernel": ([vp, C.c_int], C.c_int),
+        "sphx_get_kernel": ([vp, C.POINTER(C.c_int)], C.c_int),
         "sphx_upload": ([vp, sz, fp, fp, fp], C.c_int),
         "sphx_upload_f64": ([vp, sz, fp, fp, fp], C.c_int),
         "sphx_download_f64": ([vp, fp], C.c_int),
@@ -196,6 +202,16 @@ class Context:
 
     def set_stream(self, stream_ptr: int | None):
         self._check(self._lib.sphx_set_stream(self._h, stream_ptr or None), "sphx_set_stream")
+
+    def set_kernel(self, kernel: int):
+        """Smoothing kernel of the passes: KERNEL_CUBIC_SPLINE (the reference engine's),
+        KERNEL_WENDLAND_C2 or KERNEL_GAUSSIAN (create_kernel, src/kernels.cpp:226-236)."""
+        self._check(self._lib.sphx_set_kernel(self._h, int(kernel)), "sphx_set_kernel")
+
+    def kernel(self) -> int:
+        k = C.c_int(0)
+        self._check(self._lib.sphx_get_kernel(self._h, C.byref(k)), "sphx_get_kernel")
+        return k.value
 
     def set_params(self, p16):
         self._check(self._lib.sphx_set_params(self._h, C.byref(params_struct(p16))),

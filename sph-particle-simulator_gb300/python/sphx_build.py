@@ -75,7 +75,7 @@ def build_sphx(force: bool = False) -> Path:
     return so
 
 
-HOST_SOURCES = ["particle.cpp", "spatial_hash.cpp", "sph_engine.cpp"]
+HOST_SOURCES = ["kernels.cpp", "particle.cpp", "spatial_hash.cpp", "sph_engine.cpp"]
 HOST_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
               f"-I{REPO / 'include'}", f"-I{PKG / 'host' / 'include'}",
               "-idirafter", str(PKG / "host" / "compat")]

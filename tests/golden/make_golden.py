@@ -12,11 +12,15 @@ Cases (all arrays float32 unless noted, vectors as (n, 3)):
               outside the box, particles on cell faces, a zero-velocity-mass mix
   collapse    12x12x12 jittered lattice stepped 4 times at dt 1e-3 (the reference's
               dynamics degenerate after step 1: clamped walls, crowded cells)
+  kernel/*    W / gradW / laplacianW of create_kernel(CUBIC_SPLINE | WENDLAND_C2 | GAUSSIAN,
+              h = 0.02, 0.0137) at 167 vectors (zero, tiny, on q = 1 and q = 2, random)
   scene/*     the reference's initialize_dam_break / _fluid_drop / _granular_flow particle
               sets (default parameters): count, SHA-256 of (n, 11) float32 records
               pos3 vel3 mass type color3, and the first 8 records
 For each case: params16, pos, vel, mass; the neighbour lists of the initial state
-(counts int64, idx int32, reference order); rho/P/acc of one field evaluation; and for
+(counts int64, idx int32, reference order); rho/P/acc of one field evaluation (and, for
+lattice / exact / edge, rho_k{1,2} / pressure_k{1,2} / acc_k{1,2}: the same evaluation
+with create_kernel(WENDLAND_C2) and create_kernel(GAUSSIAN)); and for
 `steps` steps of SPHEngine::step(dt) (dt > 0 fixed, dt == 0 adaptive CFL) the positions,
 velocities, densities, pressures and current time after each step.
 """
@@ -59,6 +63,21 @@ def edge_case():
     mass[5] = 2e-3
     prm = I.params16(xmin=0.0, xmax=1.0, ymin=0.0, ymax=1.0, zmin=0.0, zmax=1.0)
     return pos, vel, mass, prm
+
+
+def kernel_sample_vectors():
+    """r vectors for the kernel-object fixture: zero, tiny (|r| < 1e-6), random directions
+    at |r| spread over [0, 2.5h] for h = 0.02 and 0.0137, and points on q = 1 and q = 2."""
+    rng = np.random.default_rng(13)
+    d = rng.standard_normal((160, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rad = np.concatenate([rng.uniform(0.0, 0.05, 120), [1e-7, 5e-7, 0.0137, 0.0274, 0.02, 0.04,
+                                                        0.04 + 1e-7, 0.0399999]])
+    rad = np.concatenate([rad, rng.uniform(0.0, 0.05, 160 - rad.size)])
+    rv = (d * rad[:, None]).astype(np.float32)
+    extra = np.array([[0, 0, 0], [0.02, 0, 0], [0, 0.04, 0], [0, 0, 0.0137], [0, 0, 0.0274],
+                      [1e-8, 0, 0], [0.01, 0.01, 0.01]], np.float32)
+    return np.ascontiguousarray(np.concatenate([rv, extra]))
 
 
 def cases():
@@ -104,6 +123,12 @@ def main():
         out[pre + "rho"] = rho
         out[pre + "pressure"] = P
         out[pre + "acc"] = acc
+        if name != "collapse":  # the other smoothing kernels of create_kernel
+            for kind in (1, 2):
+                rk, Pk, ak = ref.fields(pos, vel, mass, prm, kernel=kind)
+                out[pre + f"rho_k{kind}"] = rk
+                out[pre + f"pressure_k{kind}"] = Pk
+                out[pre + f"acc_k{kind}"] = ak
         out[pre + "dts"] = np.array(dts, np.float32)
         out[pre + "traj_pos"] = np.stack([t[0] for t in traj])
         out[pre + "traj_vel"] = np.stack([t[1] for t in traj])
@@ -129,6 +154,23 @@ def main():
         out[f"scene/{name}/sha256"] = np.frombuffer(hashlib.sha256(rec11.tobytes()).digest(), np.uint8)
         out[f"scene/{name}/first"] = rec11[:8]
         print(f"scene {name}: n={n}")
+    # the kernel objects themselves: W / gradW / laplacianW of create_kernel(kind, h)
+    L.ref_kernel_eval.argtypes = [C.c_int, C.c_float, C.c_size_t] + [C.c_void_p] * 4
+    rv = kernel_sample_vectors()
+    for kind in (0, 1, 2):
+        for h in (0.02, 0.0137):
+            m = rv.shape[0]
+            w = np.zeros(m, np.float32)
+            g = np.zeros((m, 3), np.float32)
+            lap = np.zeros(m, np.float32)
+            L.ref_kernel_eval(kind, C.c_float(h), m, rv.ctypes.data_as(C.c_void_p),
+                              w.ctypes.data_as(C.c_void_p), g.ctypes.data_as(C.c_void_p),
+                              lap.ctypes.data_as(C.c_void_p))
+            key = f"kernel/k{kind}_h{h}"
+            out[key + "/r"] = rv
+            out[key + "/W"] = w
+            out[key + "/gradW"] = g
+            out[key + "/laplacianW"] = lap
     path = Path(__file__).with_name("sph_ref_golden.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({path.stat().st_size / 1024:.0f} KiB)")

@@ -172,3 +172,26 @@ def test_grid_abi_batched_queries(port):
     assert counts[1] == 0 and counts[2] == 0
     cells, mx = g.info()
     assert cells > 0 and mx >= 1
+
+
+def test_simulator_kernel_type_matches_oracle_engine(sph, port):
+    """set_kernel_type(WENDLAND_C2): the engine's step equals the oracle engine stepping
+    with create_kernel(WENDLAND_C2); the choice survives set_smoothing_length."""
+    w = I.config0()
+    sim = sph.Simulator(w.n)
+    sim.initialize(params_obj(sph, w.params))
+    sim.set_kernel_type(sph.KernelType.WENDLAND_C2)
+    assert sim.get_kernel_type() == sph.KernelType.WENDLAND_C2
+    sim.add_particles_array(w.pos, w.vel, w.mass)
+    e = O.Engine(port, w.n)
+    e.set_kernel(1)
+    e.initialize(w.params)
+    e.add(w.pos, w.vel, w.mass)
+    for s, dt in enumerate([1e-3, 0.0, 1e-3]):
+        sim.step(dt)
+        e.step(dt)
+        ref = e.get()
+        bits(sim.get_positions(), ref["pos"], f"pos@{s}")
+        bits(sim.get_densities(), ref["rho_cap"], f"rho@{s}")
+    sim.set_smoothing_length(0.02)
+    assert sim.get_kernel_type() == sph.KernelType.WENDLAND_C2

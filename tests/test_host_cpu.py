@@ -82,3 +82,30 @@ def test_scene_generators_match_reference(sph, golden, scene):
     assert np.array_equal(rec[:8].view(np.uint32), golden[f"scene/{scene}/first"].view(np.uint32))
     digest = np.frombuffer(hashlib.sha256(rec.tobytes()).digest(), np.uint8)
     assert np.array_equal(digest, golden[f"scene/{scene}/sha256"])
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2])
+@pytest.mark.parametrize("h", [0.02, 0.0137])
+def test_kernel_objects_match_reference(sph, golden, kind, h):
+    """create_kernel(type, h)->W / gradW / laplacianW give the reference's bits
+    (fixture from the reference's own kernel classes, src/kernels.cpp:140-236)."""
+    import sph_oracle as O
+
+    key = f"kernel/k{kind}_h{h}"
+    r = golden[key + "/r"]
+    k = sph.create_kernel(sph.KernelType(kind), h)
+    w = np.array([k.W(sph.vec3(*map(float, v))) for v in r], np.float32)
+    g = np.array([[c.x, c.y, c.z] for c in (k.gradW(sph.vec3(*map(float, v))) for v in r)],
+                 np.float32)
+    lap = np.array([k.laplacianW(sph.vec3(*map(float, v))) for v in r], np.float32)
+    assert O.bits_equal(w, golden[key + "/W"]), O.mismatch_report(w, golden[key + "/W"], "W")
+    assert O.bits_equal(g, golden[key + "/gradW"]), O.mismatch_report(g, golden[key + "/gradW"], "gradW")
+    assert O.bits_equal(lap, golden[key + "/laplacianW"]), O.mismatch_report(
+        lap, golden[key + "/laplacianW"], "laplacianW")
+    assert k.get_support_radius() == np.float32(2.0) * np.float32(h)
+
+
+def test_kernel_factory_rejects_unknown_type_and_engine_default(sph):
+    with pytest.raises((ValueError, TypeError)):
+        sph.create_kernel(sph.KernelType(7), 0.02)
+    assert int(sph.KernelType.WENDLAND_C2) == 1 and int(sph.KernelType.GAUSSIAN) == 2

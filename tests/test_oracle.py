@@ -31,6 +31,17 @@ def test_port_fields_match_reference_fixture(port, golden, case):
     assert O.bits_equal(acc, g["acc"]), O.mismatch_report(acc, g["acc"], "acc")
 
 
+@pytest.mark.parametrize("kind", [1, 2])
+@pytest.mark.parametrize("case", ["lattice", "exact", "edge"])
+def test_port_kernel_variants_match_reference_fixture(port, golden, case, kind):
+    """Wendland C2 (1) and Gaussian (2) through create_kernel + equations::*."""
+    g = golden_case(golden, case)
+    rho, P, acc = port.fields(g["pos"], g["vel"], g["mass"], g["params"], kernel=kind)
+    for got, key in ((rho, "rho"), (P, "pressure"), (acc, "acc")):
+        want = g[f"{key}_k{kind}"]
+        assert O.bits_equal(got, want), O.mismatch_report(got, want, f"{key} kernel {kind}")
+
+
 @pytest.mark.parametrize("case", GOLDEN_CASES)
 def test_port_trajectory_matches_reference_fixture(port, golden, case):
     g = golden_case(golden, case)
