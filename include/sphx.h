@@ -289,6 +289,55 @@ int sphx_grid_cell(sphx_grid* grid, int x, int y, int z, int64_t* idx, size_t* c
 int sphx_density_noalloc(const sphx_params* params, size_t n, const float* pos_xyz,
                          const float* mass, float* rho, float* pressure, void* cuda_stream);
 
+/* ---- headless rendering ---------------------------------------------------------------
+ * The reference draws the particles with OpenGL as instanced camera-facing quads
+ * (Renderer::render_particles_instanced, src/renderer.cpp:314-333) shaded by
+ * shaders/particle.vert:20-40 and shaders/particle.frag:15-104.  These calls run the same
+ * vertex and fragment arithmetic as CUDA kernels on the context's particle state (insertion
+ * order) and write device buffers instead of a GL framebuffer.  No window, context or
+ * graphics API is involved. */
+#define SPHX_COLOR_VELOCITY 0 /* RenderParameters::ColorMode (src/renderer.h:43-48) */
+#define SPHX_COLOR_DENSITY 1  /* the shader's placeholder: 1000 + 200 * height */
+#define SPHX_COLOR_PRESSURE 2 /* the shader's placeholder: 5000 * |v| */
+#define SPHX_COLOR_TYPE 3     /* the particle's own colour */
+
+typedef struct {
+    float view[16];        /* column-major (GLM / GL layout) */
+    float projection[16];
+    float model[16];       /* the reference passes the identity (renderer.cpp:325) */
+    float particle_size;   /* RenderParameters::particle_size (default 0.01) */
+    int color_mode;        /* SPHX_COLOR_* */
+    int width, height;     /* image size (the viewport) */
+    float background[3];   /* RenderParameters::background_color */
+} sphx_render_params;
+
+/* Camera::update_vectors + get_view_matrix + get_projection_matrix
+ * (src/renderer.cpp:12-29): front from yaw / pitch (degrees), right = front x (0, 1, 0),
+ * up = right x front, a right-handed look-at view and an OpenGL perspective with fov
+ * (degrees), near 0.1, far 100.  Both matrices column-major. */
+void sphx_camera_matrices(const float position[3], float yaw_deg, float pitch_deg,
+                          float fov_deg, float aspect, float view[16], float projection[16]);
+
+/* Per particle (insertion order), 20 floats: the 4 billboard corners in clip space (x, y,
+ * z, w each; corner order (-,-), (+,-), (+,+), (-,+) as the reference's quad VBO,
+ * renderer.cpp:118-123) and the fragment colour RGBA.  colors: 3 floats per particle
+ * (Particle::color) or NULL for the default (0, 0.5, 1).  Host pointers; the _device form
+ * takes device pointers and is asynchronous on the context's stream. */
+int sphx_render_instances(sphx_ctx* ctx, const sphx_render_params* params,
+                          const float* colors, float* instances);
+int sphx_render_instances_device(sphx_ctx* ctx, const sphx_render_params* params,
+                                 const float* colors_dev, float* instances_dev);
+
+/* Rasterises the instances into a width x height RGBA8 image (rows bottom-up, as GL reads
+ * them back): depth test GL_LESS against the cleared 1.0 (renderer.cpp:51, 275-277),
+ * alpha 1 (so the enabled blending keeps the fragment colour), background where no quad
+ * covers a pixel centre.  Host pointers; _device as above (rgba_dev: width*height*4
+ * bytes). */
+int sphx_render_image(sphx_ctx* ctx, const sphx_render_params* params, const float* colors,
+                      unsigned char* rgba);
+int sphx_render_image_device(sphx_ctx* ctx, const sphx_render_params* params,
+                             const float* colors_dev, unsigned char* rgba_dev);
+
 #ifdef __cplusplus
 }
 #endif

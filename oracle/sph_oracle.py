@@ -109,6 +109,8 @@ class Port(_Lib):
         L.orc_engine_step_count.argtypes = [C.c_void_p]
         L.orc_max_threads.restype = C.c_int
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_render_instances.argtypes = [C.c_void_p, C.c_size_t] + [C.c_void_p] * 4
+        L.orc_render_image.argtypes = [C.c_void_p, C.c_size_t] + [C.c_void_p] * 4
 
     def fields_f64(self, pos, vel, mass, params16, want_scale: bool = False, kernel: int = 0):
         pos = _f32(pos).reshape(-1, 3)
@@ -137,6 +139,27 @@ class Port(_Lib):
         pairs = self.lib.orc_fields_f64d(n, _p(pos64), _p(vel), _p(mass), _p(prm), _p(rho),
                                          _p(P), _p(acc))
         return rho, P, acc, pairs
+
+    def render_instances(self, rp, pos, vel, colors=None):
+        """(n, 20) float32: clip-space corners and colour of every particle.  rp is a
+        sphx_render_params-layout ctypes structure."""
+        pos = _f32(pos).reshape(-1, 3)
+        n = pos.shape[0]
+        vel = _f32(vel).reshape(n, 3)
+        col = None if colors is None else _f32(colors).reshape(n, 3)
+        out = np.zeros((n, 20), np.float32)
+        self.lib.orc_render_instances(C.byref(rp), n, _p(pos), _p(vel), _p(col), _p(out))
+        return out
+
+    def render_image(self, rp, pos, vel, colors=None):
+        """(height, width, 4) uint8 image, rows bottom-up."""
+        pos = _f32(pos).reshape(-1, 3)
+        n = pos.shape[0]
+        vel = _f32(vel).reshape(n, 3)
+        col = None if colors is None else _f32(colors).reshape(n, 3)
+        img = np.zeros((rp.height, rp.width, 4), np.uint8)
+        self.lib.orc_render_image(C.byref(rp), n, _p(pos), _p(vel), _p(col), _p(img))
+        return img
 
     def threads(self) -> int:
         return self.lib.orc_max_threads()

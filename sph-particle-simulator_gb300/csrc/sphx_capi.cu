@@ -51,6 +51,13 @@ struct sphx_ctx {
     float graph_dt = 0.0f;
     int graph_launches = 0;
     uint64_t version = 0;  // bumped by every change the graph depends on
+    // headless rendering: colour staging, instance buffer, depth keys and image
+    float* r_colors = nullptr;
+    float* r_inst = nullptr;
+    size_t r_cap = 0;  // particles the two above hold
+    unsigned long long* r_keys = nullptr;
+    uchar4* r_rgba = nullptr;
+    size_t r_pix_cap = 0;
     static constexpr int kProfRing = 64;
     struct ProfSlot {
         cudaEvent_t ev[5];
@@ -208,7 +215,8 @@ void free_all(sphx_ctx* c) {
                     b.key[0], b.key[1], b.val[0], b.val[1],   b.key_s,     b.id_s,
                     b.off,  b.tile_start, b.hist, b.scan_part, b.diag_part, c->ds,
                     c->stage, c->snap_pos, c->snap_vel, c->snap_cell, b.cell4, b.cell4_s,
-                    b.scene_of, b.scene_s, b.scenes, b.hitmask, b.tile_slot};
+                    b.scene_of, b.scene_s, b.scenes, b.hitmask, b.tile_slot,
+                    c->r_colors, c->r_inst, c->r_keys, c->r_rgba};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto& slot : c->prof)
@@ -333,6 +341,78 @@ int run_step_graph(sphx_ctx* c, float dt) {
     c->launches += (uint64_t)c->graph_launches;
     c->have_fields = true;
     return SPHX_OK;
+}
+
+
+// ---- headless rendering helpers ----------------------------------------------------------
+
+// C = A * B for column-major 4x4 float matrices, each element summed k = 0..3 in order
+void mat4_mul(const float* A, const float* B, float* C) {
+    for (int col = 0; col < 4; ++col)
+        for (int row = 0; row < 4; ++row) {
+            float acc = A[row] * B[col * 4];
+            for (int k = 1; k < 4; ++k) acc = acc + A[k * 4 + row] * B[col * 4 + k];
+            C[col * 4 + row] = acc;
+        }
+}
+
+int render_const(const sphx_render_params* p, RenderConst& r) {
+    if (!p || p->width <= 0 || p->height <= 0 || p->width > 16384 || p->height > 16384 ||
+        p->color_mode < SPHX_COLOR_VELOCITY || p->color_mode > SPHX_COLOR_TYPE ||
+        !std::isfinite(p->particle_size))
+        return SPHX_ERR_INVALID_ARG;
+    float pv[16];
+    mat4_mul(p->projection, p->view, pv);
+    mat4_mul(pv, p->model, r.pvm);
+    for (int a = 0; a < 3; ++a) {
+        r.right[a] = p->view[a * 4];   // (view[0][0], view[1][0], view[2][0])
+        r.up[a] = p->view[a * 4 + 1];  // (view[0][1], view[1][1], view[2][1])
+        r.bg[a] = p->background[a];
+    }
+    r.size = p->particle_size;
+    r.mode = p->color_mode;
+    // lightDir = normalize((1, 1, 1)), normal = (0, 0, 1): diff = max(lightDir.z, 0)
+    const float len = std::sqrt((1.0f * 1.0f + 1.0f * 1.0f) + 1.0f * 1.0f);
+    const float lz = 1.0f / len;
+    r.diffuse = lz > 0.0f ? lz : 0.0f;
+    r.width = p->width;
+    r.height = p->height;
+    return SPHX_OK;
+}
+
+int render_buffers(sphx_ctx* c, size_t npix) {
+    int rc;
+    if (c->r_cap < c->capacity) {
+        if (c->r_colors) cudaFree(c->r_colors);
+        if (c->r_inst) cudaFree(c->r_inst);
+        c->r_colors = c->r_inst = nullptr;
+        c->r_cap = 0;
+        if ((rc = dmalloc(&c->r_colors, 3 * c->capacity)) ||
+            (rc = dmalloc(&c->r_inst, 20 * c->capacity)))
+            return rc;
+        c->r_cap = c->capacity;
+    }
+    if (npix > c->r_pix_cap) {
+        if (c->r_keys) cudaFree(c->r_keys);
+        if (c->r_rgba) cudaFree(c->r_rgba);
+        c->r_keys = nullptr;
+        c->r_rgba = nullptr;
+        c->r_pix_cap = 0;
+        if ((rc = dmalloc(&c->r_keys, npix)) || (rc = dmalloc(&c->r_rgba, npix))) return rc;
+        c->r_pix_cap = npix;
+    }
+    return SPHX_OK;
+}
+
+RenderArgs render_args(sphx_ctx* c, const float* colors_dev) {
+    RenderArgs a;
+    a.n = (int)c->n;
+    a.pos4 = c->b.pos4;
+    a.vel4 = c->b.vel4;
+    a.cell4 = c->b.cell4;
+    a.cs = (double)c->params.neighbor_search_radius;
+    a.colors = colors_dev;
+    return a;
 }
 
 }  // namespace
@@ -1012,6 +1092,124 @@ int sphx_debug_pairs(sphx_ctx* c, int64_t* counts, int64_t* idx, size_t* total_i
     cudaFree(d_off);
     cudaFree(d_out);
     if (e != cudaSuccess) return cuda_fail(e);
+    return SPHX_OK;
+}
+
+void sphx_camera_matrices(const float position[3], float yaw_deg, float pitch_deg,
+                          float fov_deg, float aspect, float view[16], float projection[16]) {
+    const float rad = 0.01745329251994329577f;
+    auto normalize = [](float v[3]) {
+        const float l = std::sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+        for (int a = 0; a < 3; ++a) v[a] = v[a] / l;
+    };
+    auto cross = [](const float a[3], const float b[3], float o[3]) {
+        o[0] = a[1] * b[2] - b[1] * a[2];
+        o[1] = a[2] * b[0] - b[2] * a[0];
+        o[2] = a[0] * b[1] - b[0] * a[1];
+    };
+    const float yaw = yaw_deg * rad, pitch = pitch_deg * rad;
+    float front[3] = {std::cos(yaw) * std::cos(pitch), std::sin(pitch),
+                      std::sin(yaw) * std::cos(pitch)};
+    normalize(front);
+    const float world_up[3] = {0.0f, 1.0f, 0.0f};
+    float right[3], up[3];
+    cross(front, world_up, right);
+    normalize(right);
+    cross(right, front, up);
+    normalize(up);
+    // look-at from position towards position + front: s = normalize(f x up), u = s x f
+    float f[3] = {front[0], front[1], front[2]};
+    normalize(f);
+    float sv[3], u[3];
+    cross(f, up, sv);
+    normalize(sv);
+    cross(sv, f, u);
+    const float* e = position;
+    for (int k = 0; k < 16; ++k) view[k] = (k % 5 == 0) ? 1.0f : 0.0f;
+    for (int a = 0; a < 3; ++a) {
+        view[a * 4 + 0] = sv[a];
+        view[a * 4 + 1] = u[a];
+        view[a * 4 + 2] = -f[a];
+    }
+    view[12] = -((sv[0] * e[0] + sv[1] * e[1]) + sv[2] * e[2]);
+    view[13] = -((u[0] * e[0] + u[1] * e[1]) + u[2] * e[2]);
+    view[14] = (f[0] * e[0] + f[1] * e[1]) + f[2] * e[2];
+    // perspective, depth mapped to [-1, 1] (near 0.1, far 100)
+    const float zn = 0.1f, zf = 100.0f;
+    const float t = std::tan(fov_deg * rad / 2.0f);
+    for (int k = 0; k < 16; ++k) projection[k] = 0.0f;
+    projection[0] = 1.0f / (aspect * t);
+    projection[5] = 1.0f / t;
+    projection[10] = -(zf + zn) / (zf - zn);
+    projection[11] = -1.0f;
+    projection[14] = -(2.0f * zf * zn) / (zf - zn);
+}
+
+int sphx_render_instances_device(sphx_ctx* c, const sphx_render_params* p,
+                                 const float* colors_dev, float* instances_dev) {
+    int rc = enter(c);
+    if (rc) return rc;
+    RenderConst r;
+    if ((rc = render_const(p, r))) return rc;
+    if (c->n > 0 && !instances_dev) return SPHX_ERR_INVALID_ARG;
+    c->launches += launch_render_instances(c->L, r, render_args(c, colors_dev), instances_dev);
+    SPHX_CUDA(cudaGetLastError());
+    return SPHX_OK;
+}
+
+int sphx_render_instances(sphx_ctx* c, const sphx_render_params* p, const float* colors,
+                          float* instances) {
+    int rc = enter(c);
+    if (rc) return rc;
+    RenderConst r;
+    if ((rc = render_const(p, r))) return rc;
+    if (c->n == 0) return SPHX_OK;
+    if (!instances) return SPHX_ERR_INVALID_ARG;
+    if ((rc = render_buffers(c, 0))) return rc;
+    if (colors)
+        SPHX_CUDA(cudaMemcpyAsync(c->r_colors, colors, 3 * c->n * sizeof(float),
+                                  cudaMemcpyHostToDevice, c->stream));
+    c->launches += launch_render_instances(c->L, r, render_args(c, colors ? c->r_colors : nullptr),
+                                           c->r_inst);
+    SPHX_CUDA(cudaGetLastError());
+    SPHX_CUDA(cudaMemcpyAsync(instances, c->r_inst, 20 * c->n * sizeof(float),
+                              cudaMemcpyDeviceToHost, c->stream));
+    SPHX_CUDA(cudaStreamSynchronize(c->stream));
+    return SPHX_OK;
+}
+
+int sphx_render_image_device(sphx_ctx* c, const sphx_render_params* p, const float* colors_dev,
+                             unsigned char* rgba_dev) {
+    int rc = enter(c);
+    if (rc) return rc;
+    RenderConst r;
+    if ((rc = render_const(p, r))) return rc;
+    if (!rgba_dev) return SPHX_ERR_INVALID_ARG;
+    const size_t npix = (size_t)p->width * p->height;
+    if ((rc = render_buffers(c, npix))) return rc;
+    c->launches += launch_render_image(c->L, r, render_args(c, colors_dev), c->r_keys,
+                                       reinterpret_cast<uchar4*>(rgba_dev));
+    SPHX_CUDA(cudaGetLastError());
+    return SPHX_OK;
+}
+
+int sphx_render_image(sphx_ctx* c, const sphx_render_params* p, const float* colors,
+                      unsigned char* rgba) {
+    int rc = enter(c);
+    if (rc) return rc;
+    RenderConst r;
+    if ((rc = render_const(p, r))) return rc;
+    if (!rgba) return SPHX_ERR_INVALID_ARG;
+    const size_t npix = (size_t)p->width * p->height;
+    if ((rc = render_buffers(c, npix))) return rc;
+    if (colors && c->n)
+        SPHX_CUDA(cudaMemcpyAsync(c->r_colors, colors, 3 * c->n * sizeof(float),
+                                  cudaMemcpyHostToDevice, c->stream));
+    c->launches += launch_render_image(c->L, r, render_args(c, colors ? c->r_colors : nullptr),
+                                       c->r_keys, c->r_rgba);
+    SPHX_CUDA(cudaGetLastError());
+    SPHX_CUDA(cudaMemcpyAsync(rgba, c->r_rgba, npix * 4, cudaMemcpyDeviceToHost, c->stream));
+    SPHX_CUDA(cudaStreamSynchronize(c->stream));
     return SPHX_OK;
 }
 

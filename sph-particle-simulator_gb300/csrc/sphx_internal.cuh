@@ -137,6 +137,25 @@ struct Buffers {
 };
 constexpr uint32_t kNoSlot = 0xffffffffu;
 
+// Headless rendering (sphx_render.cu): the shader pair's uniforms, derived on the host.
+struct RenderConst {
+    float pvm[16];          // projection * view * model, column-major
+    float right[3], up[3];  // camera right / up: rows 0 and 1 of the view matrix
+    float size;             // particleSize
+    int mode;               // colorMode: 0 velocity, 1 density, 2 pressure, 3 type
+    float diffuse;          // max(dot(normal, lightDir), 0) of the fragment shader
+    int width, height;      // viewport = image
+    float bg[3];            // clear colour
+};
+struct RenderArgs {
+    int n;
+    const float4* pos4;   // insertion order (precision mode: in-cell offsets)
+    const float4* vel4;
+    const int4* cell4;    // precision mode: cells (else null)
+    double cs;            // precision mode: cell size
+    const float* colors;  // per-particle colour (3 floats) or null (0, 0.5, 1)
+};
+
 // ---- exact float arithmetic: IEEE round-to-nearest, never contracted into FMA ---------
 __device__ __forceinline__ float xmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float xadd(float a, float b) { return __fadd_rn(a, b); }
@@ -297,6 +316,10 @@ void launch_unpack_sorted(const LaunchCtx& L, int n, const uint32_t* id_s,
                           const float4* aux4_s, const float4* acc4_s, float* rho,
                           float* pressure, float* acc3);
 // precision mode: absolute positions (float or double) <-> cell + offset
+int launch_render_instances(const LaunchCtx& L, const RenderConst& r, const RenderArgs& a,
+                            float* out);
+int launch_render_image(const LaunchCtx& L, const RenderConst& r, const RenderArgs& a,
+                        unsigned long long* keys, uchar4* rgba);
 void launch_pack_cells(const LaunchCtx& L, const StepConst& c, int n, const float* pos3f,
                        const double* pos3d, const float* vel3, const float* mass, int4* cell4,
                        float4* pos4, float4* vel4);

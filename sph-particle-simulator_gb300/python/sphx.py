@@ -29,6 +29,8 @@ MODE_PRECISE_FP16 = 2
 KERNEL_CUBIC_SPLINE = 0
 KERNEL_WENDLAND_C2 = 1
 KERNEL_GAUSSIAN = 2
+# render colour modes (RenderParameters::ColorMode order)
+COLOR_VELOCITY, COLOR_DENSITY, COLOR_PRESSURE, COLOR_TYPE = 0, 1, 2, 3
 
 # every symbol include/sphx.h declares
 EXPORTS = (
@@ -39,7 +41,9 @@ EXPORTS = (
     "sphx_snapshot", "sphx_restore", "sphx_debug_pairs", "sphx_grid_create",
     "sphx_grid_destroy", "sphx_grid_build", "sphx_grid_query", "sphx_grid_info",
     "sphx_grid_cell", "sphx_set_scenes", "sphx_get_scene_stats", "sphx_autotune",
-    "sphx_density_noalloc", "sphx_set_kernel", "sphx_get_kernel",
+    "sphx_density_noalloc", "sphx_set_kernel", "sphx_get_kernel", "sphx_camera_matrices",
+    "sphx_render_instances", "sphx_render_instances_device", "sphx_render_image",
+    "sphx_render_image_device",
 )
 NOALLOC_MAX_PARTICLES = 65536
 
@@ -85,6 +89,42 @@ class SphxStats(C.Structure):
         return d
 
 
+class SphxRenderParams(C.Structure):
+    """sphx_render_params: column-major view / projection / model, particle size, colour
+    mode, image size, background colour."""
+    _fields_ = [("view", C.c_float * 16), ("projection", C.c_float * 16),
+                ("model", C.c_float * 16), ("particle_size", C.c_float),
+                ("color_mode", C.c_int), ("width", C.c_int), ("height", C.c_int),
+                ("background", C.c_float * 3)]
+
+
+def camera_matrices(position=(0.0, 0.0, 3.0), yaw=-90.0, pitch=0.0, fov=45.0,
+                    aspect=1280 / 720):
+    """view, projection (16 float32 each, column-major) of the reference's Camera
+    (src/renderer.h:16-29, renderer.cpp:12-29) -- defaults are its defaults."""
+    v = (C.c_float * 16)()
+    p = (C.c_float * 16)()
+    pos = (C.c_float * 3)(*position)
+    lib().sphx_camera_matrices(pos, C.c_float(yaw), C.c_float(pitch), C.c_float(fov),
+                               C.c_float(aspect), v, p)
+    return np.frombuffer(v, np.float32).copy(), np.frombuffer(p, np.float32).copy()
+
+
+def render_params(view, projection, model=None, particle_size=0.01, color_mode=0,
+                  width=1280, height=720, background=(0.1, 0.1, 0.15)) -> SphxRenderParams:
+    """Render parameters (defaults: the reference's RenderParameters, src/renderer.h:32-56)."""
+    rp = SphxRenderParams()
+    rp.view[:] = [float(x) for x in np.asarray(view, np.float32).ravel()]
+    rp.projection[:] = [float(x) for x in np.asarray(projection, np.float32).ravel()]
+    m = np.eye(4, dtype=np.float32) if model is None else np.asarray(model, np.float32)
+    rp.model[:] = [float(x) for x in m.ravel()]
+    rp.particle_size = particle_size
+    rp.color_mode = color_mode
+    rp.width, rp.height = width, height
+    rp.background[:] = [float(x) for x in background]
+    return rp
+
+
 class SphxError(RuntimeError):
     def __init__(self, code: int, where: str):
         super().__init__(f"{where}: {ERRORS.get(code, code)} ({code})")
@@ -105,6 +145,11 @@ def load_library(path: Path | str = LIB_PATH) -> C.CDLL:
         "sphx_set_stream": ([vp, vp], C.c_int),
         "sphx_set_params": ([vp, C.POINTER(SphxParams)], C.c_int),
         "sphx_set_kernel": ([vp, C.c_int], C.c_int),
+        "sphx_camera_matrices": ([fp, C.c_float, C.c_float, C.c_float, C.c_float, fp, fp], None),
+        "sphx_render_instances": ([vp, C.POINTER(SphxRenderParams), fp, fp], C.c_int),
+        "sphx_render_instances_device": ([vp, C.POINTER(SphxRenderParams), fp, fp], C.c_int),
+        "sphx_render_image": ([vp, C.POINTER(SphxRenderParams), fp, fp], C.c_int),
+        "sphx_render_image_device": ([vp, C.POINTER(SphxRenderParams), fp, fp], C.c_int),
         "sphx_get_kernel": ([vp, C.POINTER(C.c_int)], C.c_int),
         "sphx_upload": ([vp, sz, fp, fp, fp], C.c_int),
         "sphx_upload_f64": ([vp, sz, fp, fp, fp], C.c_int),
@@ -202,6 +247,24 @@ class Context:
 
     def set_stream(self, stream_ptr: int | None):
         self._check(self._lib.sphx_set_stream(self._h, stream_ptr or None), "sphx_set_stream")
+
+    def render_instances(self, rp: SphxRenderParams, colors=None) -> np.ndarray:
+        """(n, 20) float32: 4 clip-space corners (x, y, z, w) and RGBA per particle."""
+        n = self.size()
+        out = np.zeros((n, 20), np.float32)
+        col = None if colors is None else np.ascontiguousarray(colors, np.float32).reshape(n, 3)
+        self._check(self._lib.sphx_render_instances(self._h, C.byref(rp), _ptr(col), _ptr(out)),
+                    "sphx_render_instances")
+        return out
+
+    def render_image(self, rp: SphxRenderParams, colors=None) -> np.ndarray:
+        """(height, width, 4) uint8 RGBA image, rows bottom-up (GL order)."""
+        n = self.size()
+        img = np.zeros((rp.height, rp.width, 4), np.uint8)
+        col = None if colors is None else np.ascontiguousarray(colors, np.float32).reshape(n, 3)
+        self._check(self._lib.sphx_render_image(self._h, C.byref(rp), _ptr(col), _ptr(img)),
+                    "sphx_render_image")
+        return img
 
     def set_kernel(self, kernel: int):
         """Smoothing kernel of the passes: KERNEL_CUBIC_SPLINE (the reference engine's),

@@ -26,7 +26,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
               "-ffp-contract=off", "-Xptxas", "-warn-spills", f"-I{REPO / 'include'}"]
 CUDA_SOURCES = ["sphx_sort.cu", "sphx_grid.cu", "sphx_passes.cu", "sphx_batch.cu",
-                "sphx_capi.cu", "sphx_hash.cu", "sphx_noalloc.cu"]
+                "sphx_capi.cu", "sphx_hash.cu", "sphx_noalloc.cu",
+                "sphx_render.cu"]
 
 
 def _nvcc() -> str:
@@ -130,12 +131,12 @@ def build_oracle(force: bool = False) -> Path:
     """Compiles the C restatement of the reference step (test infrastructure)."""
     out_dir = REPO / "oracle" / "_build"
     out_dir.mkdir(exist_ok=True)
-    src = REPO / "oracle" / "sph_oracle.c"
+    srcs = [REPO / "oracle" / "sph_oracle.c", REPO / "oracle" / "render_oracle.c"]
     so = out_dir / "libsph_oracle.so"
-    if force or _stale(so, [src, REPO / "oracle" / "sph_oracle.h"]):
+    if force or _stale(so, srcs + [REPO / "oracle" / "sph_oracle.h"]):
         _run_parallel([["gcc", "-std=c11", "-D_GNU_SOURCE", "-O2", "-fopenmp",
                         "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-                        str(src), "-o", str(so), "-lm"]])
+                        *map(str, srcs), "-o", str(so), "-lm"]])
     return so
 
 

@@ -109,3 +109,34 @@ def test_kernel_factory_rejects_unknown_type_and_engine_default(sph):
     with pytest.raises((ValueError, TypeError)):
         sph.create_kernel(sph.KernelType(7), 0.02)
     assert int(sph.KernelType.WENDLAND_C2) == 1 and int(sph.KernelType.GAUSSIAN) == 2
+
+
+def test_camera_matrices_follow_the_gl_conventions(built):
+    """sphx_camera_matrices (host code): look-at of the reference's Camera and an OpenGL
+    perspective (near 0.1, far 100), checked against the textbook formulas in FP64."""
+    import sphx
+
+    for pos, yaw, pitch, fov, aspect in [((0, 0, 3), -90, 0, 45, 16 / 9),
+                                         ((1.8, 1.2, 1.6), -135, -25, 35, 4 / 3)]:
+        view, proj = sphx.camera_matrices(pos, yaw, pitch, fov, aspect)
+        V = view.reshape(4, 4).T.astype(np.float64)  # column-major -> row-major
+        Pm = proj.reshape(4, 4).T.astype(np.float64)
+        y, p = np.radians(yaw), np.radians(pitch)
+        f = np.array([np.cos(y) * np.cos(p), np.sin(p), np.sin(y) * np.cos(p)])
+        f /= np.linalg.norm(f)
+        s = np.cross(f, [0, 1, 0])
+        s /= np.linalg.norm(s)
+        u = np.cross(s, f)
+        e = np.array(pos, np.float64)
+        want_v = np.eye(4)
+        want_v[0, :3], want_v[1, :3], want_v[2, :3] = s, u, -f
+        want_v[:3, 3] = [-s @ e, -u @ e, f @ e]
+        assert np.abs(V - want_v).max() < 1e-5
+        t = np.tan(np.radians(fov) / 2)
+        want_p = np.zeros((4, 4))
+        want_p[0, 0], want_p[1, 1] = 1 / (aspect * t), 1 / t
+        want_p[2, 2], want_p[2, 3], want_p[3, 2] = -100.1 / 99.9, -2 * 100 * 0.1 / 99.9, -1
+        assert np.abs(Pm - want_p).max() < 1e-5 * np.abs(want_p).max()
+        # the eye maps to the view-space origin, a point ahead of it to -z
+        assert np.abs(V @ np.append(e, 1))[:3].max() < 1e-5
+        assert (V @ np.append(e + f, 1))[2] == pytest.approx(-1.0, abs=1e-5)
