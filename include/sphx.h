@@ -289,6 +289,45 @@ int sphx_grid_cell(sphx_grid* grid, int x, int y, int z, int64_t* idx, size_t* c
 int sphx_density_noalloc(const sphx_params* params, size_t n, const float* pos_xyz,
                          const float* mass, float* rho, float* pressure, void* cuda_stream);
 
+/* ---- initial conditions generated on the device ---------------------------------------
+ * Replaces the particle set (like sphx_upload) with particles generated on the GPU, shape
+ * after shape in the given order, each shape's particles in its generator's order: the
+ * same positions, bit for bit, as the host generators (the reference's, or the project's
+ * benchmark generators), without host generation or host-to-device copies. */
+#define SPHX_SHAPE_BLOCK 0   /* create_fluid_block (src/particle.cpp:166-187) */
+#define SPHX_SHAPE_BOX 1     /* create_boundary_box (src/particle.cpp:189-226) */
+#define SPHX_SHAPE_SPHERE 2  /* create_fluid_drop_setup's ball (src/sph_engine.cpp:492-515) */
+#define SPHX_SHAPE_LATTICE 3 /* jittered lattice float32(i)*spacing + (2u-1)*jitter (+origin),
+                                u = splitmix64 uniform of (seed, index, axis) */
+#define SPHX_SHAPE_BALL 4    /* lattice points c + k*spacing (k integer vector, |k_a| <=
+                                int(R/spacing) + 1) with |k*spacing|^2 <= R^2, in FP64 */
+
+typedef struct {
+    int kind;             /* SPHX_SHAPE_* */
+    float center[3];      /* BLOCK / BOX / SPHERE centre; LATTICE origin */
+    float size[3];        /* BLOCK / BOX extents; SPHERE: size[0] = radius */
+    float spacing;        /* BLOCK / BOX / SPHERE / LATTICE */
+    float mass;           /* every particle's mass */
+    float velocity[3];    /* every particle's velocity */
+    int counts[3];        /* LATTICE: nx, ny, nz (i along x outermost, k along z innermost) */
+    float jitter;         /* LATTICE: 0 for none */
+    uint64_t seed;        /* LATTICE */
+    double ball_center[3];  /* BALL */
+    double ball_radius;     /* BALL */
+    double ball_spacing;    /* BALL */
+} sphx_shape;
+
+/* Total > capacity -> SPHX_ERR_CAPACITY and the particle set is left as it was.
+ * n_out (may be NULL) receives the number of particles. */
+int sphx_generate(sphx_ctx* ctx, size_t nshapes, const sphx_shape* shapes, size_t* n_out);
+
+/* The reference's three scenes (SPHEngine::initialize_dam_break / _fluid_drop /
+ * _granular_flow, src/sph_engine.cpp:35-71, with their arguments), particle mass given. */
+#define SPHX_SCENE_DAM_BREAK 0
+#define SPHX_SCENE_FLUID_DROP 1
+#define SPHX_SCENE_GRANULAR_FLOW 2
+int sphx_generate_scene(sphx_ctx* ctx, int scene, float particle_mass, size_t* n_out);
+
 /* ---- headless rendering ---------------------------------------------------------------
  * The reference draws the particles with OpenGL as instanced camera-facing quads
  * (Renderer::render_particles_instanced, src/renderer.cpp:314-333) shaded by

@@ -1,6 +1,7 @@
 // C ABI of the sm_103a SPH step (include/sphx.h): context lifetime, device memory,
 // host<->device transfers and the step's launch sequence.
 #include <cmath>
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -413,6 +414,102 @@ RenderArgs render_args(sphx_ctx* c, const float* colors_dev) {
     a.cs = (double)c->params.neighbor_search_radius;
     a.colors = colors_dev;
     return a;
+}
+
+
+// ---- device generation helpers -----------------------------------------------------------
+
+// The host-side constants of one shape, computed with the generator's float operations
+// (glm vector ops are component-wise; int * float converts the int first).
+int gen_shape(const sphx_shape& in, GenShape& g) {
+    std::memset(&g, 0, sizeof(g));
+    g.kind = in.kind;
+    g.spacing = in.spacing;
+    g.mass = in.mass;
+    for (int a = 0; a < 3; ++a) g.vel[a] = in.velocity[a];
+    const float sp = in.spacing;
+    auto lattice_count = [](const int n[3]) -> uint64_t {
+        if (n[0] <= 0 || n[1] <= 0 || n[2] <= 0) return 0;
+        return (uint64_t)n[0] * (uint64_t)n[1] * (uint64_t)n[2];
+    };
+    switch (in.kind) {
+        case SPHX_SHAPE_BLOCK: {
+            if (!(sp > 0.0f) || !std::isfinite(sp)) return SPHX_ERR_INVALID_ARG;
+            for (int a = 0; a < 3; ++a) {
+                g.n[a] = static_cast<int>(in.size[a] / sp);
+                g.start[a] = in.center[a] - in.size[a] * 0.5f;
+            }
+            const uint64_t c = lattice_count(g.n);
+            if (c > 0xffffffffull) return SPHX_ERR_CAPACITY;
+            g.count = (uint32_t)c;
+            return SPHX_OK;
+        }
+        case SPHX_SHAPE_BOX: {
+            if (!(sp > 0.0f) || !std::isfinite(sp)) return SPHX_ERR_INVALID_ARG;
+            float half[3];
+            for (int a = 0; a < 3; ++a) {
+                half[a] = in.size[a] * 0.5f;
+                g.start[a] = in.center[a] - half[a];
+            }
+            // faces in the reference's order: z = start.z, z = start.z + size.z,
+            // x = start.x, x = start.x + size.x, y = start.y, y = start.y + size.y
+            const int axes[6][3] = {{0, 1, 2}, {0, 1, 2}, {1, 2, 0}, {1, 2, 0}, {0, 2, 1}, {0, 2, 1}};
+            uint64_t off = 0;
+            for (int f = 0; f < 6; ++f) {
+                for (int a = 0; a < 3; ++a) g.face_a[f][a] = axes[f][a];
+                const int a3 = axes[f][2];
+                g.face_val[f] = (f % 2 == 0) ? g.start[a3] : g.start[a3] + in.size[a3];
+                const int n1 = static_cast<int>(in.size[axes[f][0]] / sp);
+                const int n2 = static_cast<int>(in.size[axes[f][1]] / sp);
+                g.face_n2[f] = n2 > 0 ? n2 : 1;
+                g.face_off[f] = (uint32_t)off;
+                if (n1 > 0 && n2 > 0) off += (uint64_t)n1 * (uint64_t)n2;
+                if (off > 0xffffffffull) return SPHX_ERR_CAPACITY;
+            }
+            g.face_off[6] = (uint32_t)off;
+            g.count = (uint32_t)off;
+            return SPHX_OK;
+        }
+        case SPHX_SHAPE_SPHERE: {
+            if (!(sp > 0.0f) || !std::isfinite(sp)) return SPHX_ERR_INVALID_ARG;
+            const float r = in.size[0];
+            const int nd = static_cast<int>(2.0f * r / sp);
+            if (nd > 4096) return SPHX_ERR_CAPACITY;
+            g.n[0] = g.n[1] = g.n[2] = nd > 0 ? nd : 0;
+            for (int a = 0; a < 3; ++a) {
+                g.center[a] = in.center[a];
+                g.start[a] = in.center[a] - r;
+            }
+            g.r2 = r * r;
+            return SPHX_OK;  // count: on the device
+        }
+        case SPHX_SHAPE_LATTICE: {
+            for (int a = 0; a < 3; ++a) {
+                g.n[a] = in.counts[a];
+                g.origin[a] = in.center[a];
+                if (in.center[a] != 0.0f) g.has_origin = 1;
+            }
+            g.jitter = in.jitter;
+            g.seed = in.seed;
+            const uint64_t c = lattice_count(g.n);
+            if (c > 0xffffffffull) return SPHX_ERR_CAPACITY;
+            g.count = (uint32_t)c;
+            return SPHX_OK;
+        }
+        case SPHX_SHAPE_BALL: {
+            const double R = in.ball_radius, bs = in.ball_spacing;
+            if (!(bs > 0.0) || !(R >= 0.0) || !std::isfinite(R / bs)) return SPHX_ERR_INVALID_ARG;
+            const double kq = R / bs;
+            if (kq > 2000.0) return SPHX_ERR_CAPACITY;
+            g.kmax = static_cast<int>(kq) + 1;
+            g.n[0] = g.n[1] = g.n[2] = 2 * g.kmax + 1;
+            for (int a = 0; a < 3; ++a) g.c64[a] = in.ball_center[a];
+            g.sp64 = bs;
+            g.R2 = R * R;
+            return SPHX_OK;
+        }
+    }
+    return SPHX_ERR_INVALID_ARG;
 }
 
 }  // namespace
@@ -1211,6 +1308,118 @@ int sphx_render_image(sphx_ctx* c, const sphx_render_params* p, const float* col
     SPHX_CUDA(cudaMemcpyAsync(rgba, c->r_rgba, npix * 4, cudaMemcpyDeviceToHost, c->stream));
     SPHX_CUDA(cudaStreamSynchronize(c->stream));
     return SPHX_OK;
+}
+
+int sphx_generate(sphx_ctx* c, size_t nshapes, const sphx_shape* shapes, size_t* n_out) {
+    int rc = enter(c);
+    if (rc) return rc;
+    if (nshapes > 0 && !shapes) return SPHX_ERR_INVALID_ARG;
+    if (c->b.cell4 && !c->have_params) return SPHX_ERR_NOT_READY;  // cells need the cell size
+    float* s_pos = c->stage;
+    float* s_vel = c->stage + 3 * c->capacity;
+    float* s_mass = c->stage + 6 * c->capacity;
+    std::vector<GenShape> gs(nshapes);
+    uint64_t max_rows = 0;
+    for (size_t k = 0; k < nshapes; ++k) {
+        if ((rc = gen_shape(shapes[k], gs[k]))) return rc;
+        if (gs[k].kind == SPHX_SHAPE_SPHERE || gs[k].kind == SPHX_SHAPE_BALL)
+            max_rows = std::max<uint64_t>(max_rows, (uint64_t)gs[k].n[0] * gs[k].n[1]);
+    }
+    uint32_t* rows = nullptr;
+    if (max_rows && (rc = dmalloc(&rows, (size_t)max_rows + 1))) return rc;
+    uint64_t total = 0;
+    for (size_t k = 0; k < nshapes && !rc; ++k) {
+        GenArgs g{gs[k], s_pos, s_vel, s_mass};
+        const bool ball = g.s.kind == SPHX_SHAPE_SPHERE || g.s.kind == SPHX_SHAPE_BALL;
+        if (ball) {
+            const uint32_t nrows = (uint32_t)g.s.n[0] * (uint32_t)g.s.n[1];
+            uint32_t cnt = 0;
+            if (nrows) {
+                launch_ball_count(c->L, g, rows);
+                cudaError_t e = cudaMemcpyAsync(&cnt, rows + nrows, sizeof(uint32_t),
+                                                cudaMemcpyDeviceToHost, c->stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+                if (e != cudaSuccess) rc = cuda_fail(e);
+            }
+            g.s.count = cnt;
+        }
+        if (rc) break;
+        if (total + g.s.count > c->capacity) {
+            rc = SPHX_ERR_CAPACITY;
+            break;
+        }
+        g.s.offset = (uint32_t)total;
+        if (g.s.count) launch_generate(c->L, g, rows);
+        total += g.s.count;
+    }
+    if (!rc) {
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = cuda_fail(e);
+    }
+    if (rows) {
+        cudaStreamSynchronize(c->stream);
+        cudaFree(rows);
+    }
+    if (rc) return rc;
+    const size_t n = (size_t)total;
+    if (n > 0) {
+        if (c->b.cell4) {
+            fill_step_const(c);
+            launch_pack_cells(c->L, c->sc, (int)n, s_pos, nullptr, s_vel, s_mass, c->b.cell4,
+                              c->b.pos4, c->b.vel4);
+        } else {
+            launch_pack(c->L, (int)n, s_pos, s_vel, s_mass, c->b.pos4, c->b.vel4);
+        }
+        SPHX_CUDA(cudaGetLastError());
+    }
+    c->n = n;
+    c->have_fields = false;
+    c->b.nscenes = 0;
+    c->nscenes = 0;
+    c->version++;
+    if (n_out) *n_out = n;
+    return SPHX_OK;
+}
+
+int sphx_generate_scene(sphx_ctx* c, int scene, float particle_mass, size_t* n_out) {
+    sphx_shape sh[2];
+    std::memset(sh, 0, sizeof(sh));
+    auto set3 = [](float* d, float x, float y, float z) { d[0] = x, d[1] = y, d[2] = z; };
+    size_t ns = 0;
+    if (scene == SPHX_SCENE_DAM_BREAK) {
+        // create_dam_break_setup(dam (0.4, 0.6, 0.8), fluid (0.2, 0.4, 0.8), 0.01)
+        const float dam[3] = {0.4f, 0.6f, 0.8f}, fluid[3] = {0.2f, 0.4f, 0.8f}, sp = 0.01f;
+        sh[0].kind = SPHX_SHAPE_BOX;
+        set3(sh[0].center, 0.0f, dam[1] / 2.0f, 0.0f);
+        set3(sh[0].size, dam[0], dam[1], dam[2]);
+        sh[1].kind = SPHX_SHAPE_BLOCK;
+        set3(sh[1].center, -dam[0] / 2.0f + fluid[0] / 2.0f, fluid[1] / 2.0f, 0.0f);
+        set3(sh[1].size, fluid[0], fluid[1], fluid[2]);
+        sh[0].spacing = sh[1].spacing = sp;
+        ns = 2;
+    } else if (scene == SPHX_SCENE_FLUID_DROP) {
+        // create_fluid_drop_setup(centre (0, 0.5, 0), radius 0.1, spacing 0.008)
+        sh[0].kind = SPHX_SHAPE_SPHERE;
+        set3(sh[0].center, 0.0f, 0.5f, 0.0f);
+        sh[0].size[0] = 0.1f;
+        sh[0].spacing = 0.008f;
+        ns = 1;
+    } else if (scene == SPHX_SCENE_GRANULAR_FLOW) {
+        // create_granular_flow_setup(pile (0.3, 0.4, 0.8), domain (1, 1, 1), 0.012)
+        const float pile[3] = {0.3f, 0.4f, 0.8f}, dom[3] = {1.0f, 1.0f, 1.0f}, sp = 0.012f;
+        sh[0].kind = SPHX_SHAPE_BOX;
+        set3(sh[0].center, 0.0f, dom[1] / 2.0f, 0.0f);
+        set3(sh[0].size, dom[0], dom[1], dom[2]);
+        sh[1].kind = SPHX_SHAPE_BLOCK;
+        set3(sh[1].center, 0.0f, pile[1] / 2.0f + sp, 0.0f);
+        set3(sh[1].size, pile[0], pile[1], pile[2]);
+        sh[0].spacing = sh[1].spacing = sp;
+        ns = 2;
+    } else {
+        return SPHX_ERR_INVALID_ARG;
+    }
+    for (size_t k = 0; k < ns; ++k) sh[k].mass = particle_mass;
+    return sphx_generate(c, ns, sh, n_out);
 }
 
 }  // extern "C"

@@ -137,6 +137,31 @@ struct Buffers {
 };
 constexpr uint32_t kNoSlot = 0xffffffffu;
 
+// Device generation of initial conditions (sphx_gen.cu): one shape, its constants derived
+// on the host with the generator's float operations.
+struct GenShape {
+    int kind;                 // SPHX_SHAPE_*
+    uint32_t offset, count;   // first staged particle; particles (balls: after counting)
+    float start[3], center[3], r2, spacing, mass, vel[3];
+    int n[3];                 // lattice extents (balls: points per axis of the cube)
+    uint32_t face_off[7];     // box: first particle of each face
+    int face_n2[6];
+    int face_a[6][3];         // box: (axis1, axis2, axis3) per face
+    float face_val[6];
+    float jitter;             // benchmark lattice
+    uint64_t seed;
+    float origin[3];
+    int has_origin;
+    double c64[3], sp64, R2;  // FP64 ball
+    int kmax;
+};
+struct GenArgs {
+    GenShape s;
+    float* pos;   // staging: 3 floats per particle
+    float* vel;
+    float* mass;
+};
+
 // Headless rendering (sphx_render.cu): the shader pair's uniforms, derived on the host.
 struct RenderConst {
     float pvm[16];          // projection * view * model, column-major
@@ -316,6 +341,8 @@ void launch_unpack_sorted(const LaunchCtx& L, int n, const uint32_t* id_s,
                           const float4* aux4_s, const float4* acc4_s, float* rho,
                           float* pressure, float* acc3);
 // precision mode: absolute positions (float or double) <-> cell + offset
+int launch_ball_count(const LaunchCtx& L, const GenArgs& g, uint32_t* rows);
+int launch_generate(const LaunchCtx& L, const GenArgs& g, const uint32_t* rows);
 int launch_render_instances(const LaunchCtx& L, const RenderConst& r, const RenderArgs& a,
                             float* out);
 int launch_render_image(const LaunchCtx& L, const RenderConst& r, const RenderArgs& a,

@@ -31,6 +31,9 @@ KERNEL_WENDLAND_C2 = 1
 KERNEL_GAUSSIAN = 2
 # render colour modes (RenderParameters::ColorMode order)
 COLOR_VELOCITY, COLOR_DENSITY, COLOR_PRESSURE, COLOR_TYPE = 0, 1, 2, 3
+# device generation (sphx_shape kinds, reference scenes)
+SHAPE_BLOCK, SHAPE_BOX, SHAPE_SPHERE, SHAPE_LATTICE, SHAPE_BALL = 0, 1, 2, 3, 4
+SCENE_DAM_BREAK, SCENE_FLUID_DROP, SCENE_GRANULAR_FLOW = 0, 1, 2
 
 # every symbol include/sphx.h declares
 EXPORTS = (
@@ -43,7 +46,7 @@ EXPORTS = (
     "sphx_grid_cell", "sphx_set_scenes", "sphx_get_scene_stats", "sphx_autotune",
     "sphx_density_noalloc", "sphx_set_kernel", "sphx_get_kernel", "sphx_camera_matrices",
     "sphx_render_instances", "sphx_render_instances_device", "sphx_render_image",
-    "sphx_render_image_device",
+    "sphx_render_image_device", "sphx_generate", "sphx_generate_scene",
 )
 NOALLOC_MAX_PARTICLES = 65536
 
@@ -87,6 +90,31 @@ class SphxStats(C.Structure):
             v = getattr(self, name)
             d[name] = list(v) if name == "momentum" else v
         return d
+
+
+class SphxShape(C.Structure):
+    """sphx_shape: one primitive of a device-generated particle set."""
+    _fields_ = [("kind", C.c_int), ("center", C.c_float * 3), ("size", C.c_float * 3),
+                ("spacing", C.c_float), ("mass", C.c_float), ("velocity", C.c_float * 3),
+                ("counts", C.c_int * 3), ("jitter", C.c_float), ("seed", C.c_uint64),
+                ("ball_center", C.c_double * 3), ("ball_radius", C.c_double),
+                ("ball_spacing", C.c_double)]
+
+
+def shape(kind, center=(0.0, 0.0, 0.0), size=(0.0, 0.0, 0.0), spacing=0.01, mass=1e-3,
+          velocity=(0.0, 0.0, 0.0), counts=(0, 0, 0), jitter=0.0, seed=0,
+          ball_center=(0.0, 0.0, 0.0), ball_radius=0.0, ball_spacing=0.0) -> SphxShape:
+    s = SphxShape()
+    s.kind = kind
+    s.center[:] = [float(x) for x in center]
+    s.size[:] = [float(x) for x in size]
+    s.spacing, s.mass = spacing, mass
+    s.velocity[:] = [float(x) for x in velocity]
+    s.counts[:] = [int(x) for x in counts]
+    s.jitter, s.seed = jitter, int(seed)
+    s.ball_center[:] = [float(x) for x in ball_center]
+    s.ball_radius, s.ball_spacing = float(ball_radius), float(ball_spacing)
+    return s
 
 
 class SphxRenderParams(C.Structure):
@@ -146,6 +174,8 @@ def load_library(path: Path | str = LIB_PATH) -> C.CDLL:
         "sphx_set_params": ([vp, C.POINTER(SphxParams)], C.c_int),
         "sphx_set_kernel": ([vp, C.c_int], C.c_int),
         "sphx_camera_matrices": ([fp, C.c_float, C.c_float, C.c_float, C.c_float, fp, fp], None),
+        "sphx_generate": ([vp, sz, C.POINTER(SphxShape), C.POINTER(sz)], C.c_int),
+        "sphx_generate_scene": ([vp, C.c_int, C.c_float, C.POINTER(sz)], C.c_int),
         "sphx_render_instances": ([vp, C.POINTER(SphxRenderParams), fp, fp], C.c_int),
         "sphx_render_instances_device": ([vp, C.POINTER(SphxRenderParams), fp, fp], C.c_int),
         "sphx_render_image": ([vp, C.POINTER(SphxRenderParams), fp, fp], C.c_int),
@@ -247,6 +277,21 @@ class Context:
 
     def set_stream(self, stream_ptr: int | None):
         self._check(self._lib.sphx_set_stream(self._h, stream_ptr or None), "sphx_set_stream")
+
+    def generate(self, shapes) -> int:
+        """Replaces the particle set with the shapes' particles, generated on the GPU."""
+        arr = (SphxShape * max(len(shapes), 1))(*shapes)
+        n = C.c_size_t(0)
+        self._check(self._lib.sphx_generate(self._h, len(shapes), arr, C.byref(n)),
+                    "sphx_generate")
+        return n.value
+
+    def generate_scene(self, scene: int, particle_mass: float = 1e-3) -> int:
+        """The reference's initialize_dam_break / _fluid_drop / _granular_flow particle set."""
+        n = C.c_size_t(0)
+        self._check(self._lib.sphx_generate_scene(self._h, int(scene), C.c_float(particle_mass),
+                                                  C.byref(n)), "sphx_generate_scene")
+        return n.value
 
     def render_instances(self, rp: SphxRenderParams, colors=None) -> np.ndarray:
         """(n, 20) float32: 4 clip-space corners (x, y, z, w) and RGBA per particle."""

@@ -27,7 +27,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
               "-ffp-contract=off", "-Xptxas", "-warn-spills", f"-I{REPO / 'include'}"]
 CUDA_SOURCES = ["sphx_sort.cu", "sphx_grid.cu", "sphx_passes.cu", "sphx_batch.cu",
                 "sphx_capi.cu", "sphx_hash.cu", "sphx_noalloc.cu",
-                "sphx_render.cu"]
+                "sphx_render.cu", "sphx_gen.cu"]
 
 
 def _nvcc() -> str:

@@ -222,6 +222,26 @@ def fluid_drop_scene(target: int, r_frac: float, h_frac: float, v_down: float, s
     return pos, vel, prm, L
 
 
+def fluid_drop_scene_shapes(target: int, r_frac: float, h_frac: float, v_down: float,
+                            seed: int, spacing: float = 0.01) -> list:
+    """The same scene as fluid_drop_scene, as two device-generator shapes (sphx_shape):
+    the pool lattice and the FP64 lattice ball (same arithmetic, same order)."""
+    import sphx
+
+    per_vol = 1.0 / spacing ** 3
+    L = (target / (per_vol * (0.3 + 4.0 / 3.0 * math.pi * r_frac ** 3))) ** (1.0 / 3.0)
+    nx = max(1, int(round(L / spacing)))
+    ny = max(1, int(round(0.3 * L / spacing)))
+    org = np.float32(spacing / 2)
+    pool = sphx.shape(sphx.SHAPE_LATTICE, center=(org, org, org), spacing=spacing,
+                      counts=(nx, ny, nx), jitter=5e-4, seed=seed, mass=1e-3)
+    R = r_frac * L
+    ball = sphx.shape(sphx.SHAPE_BALL, mass=1e-3, velocity=(0.0, -np.float32(v_down), 0.0),
+                      ball_center=(L / 2, h_frac * L, L / 2), ball_radius=R,
+                      ball_spacing=spacing)
+    return [pool, ball]
+
+
 def batched_fluid_drops(nscenes: int = 256, seed: int = 3, n_min: int = 2000,
                         n_max: int = 200000) -> Batch:
     """The batched fluid-drop mix: scene sizes log-uniform in [n_min, n_max] (about 11M
@@ -237,7 +257,9 @@ def batched_fluid_drops(nscenes: int = 256, seed: int = 3, n_min: int = 2000,
         P.append(pos)
         V.append(vel)
         params.append(prm)
-        info.append(dict(target=int(sizes[s]), n=int(pos.shape[0]), box=L))
+        info.append(dict(target=int(sizes[s]), n=int(pos.shape[0]), box=L,
+                         args=(int(sizes[s]), 0.05 + 0.10 * u[1][s], 0.6 + 0.3 * u[2][s],
+                               2.0 * u[3][s], seed * 1000 + s)))
         start.append(start[-1] + pos.shape[0])
     pos = np.concatenate(P)
     return Batch(pos=pos, vel=np.concatenate(V), mass=np.full(pos.shape[0], 1e-3, np.float32),
