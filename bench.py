@@ -2,7 +2,7 @@
 """Benchmark of the GB300 SPH step (one JSON line on stdout).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload dam_break_1M|dam_break_10M|dam_break_10k]
+                  [--workload dam_break_1M|dam_break_4M|dam_break_10M|dam_break_10k]
 
 A "step" is one SPHEngine::step over the workload's particles.  Protocol: fresh-state
 (every step starts from the workload's initial state, restored on the device before the
@@ -18,8 +18,15 @@ describes.  Between timed steps the L2 cache is flushed (a 512 MiB buffer is wri
   roofline   the force+integrate kernel (the dominant kernel): algorithmic bytes per launch
              (72 B per particle) over its average CUDA-event duration, against the measured
              HBM copy bandwidth
+  roofline_issue  the same kernel against the issue roof (it is instruction-issue bound):
+             warp instructions per particle (ncu, profiles/ncu_issue.json) x particles over
+             the kernel time, against SMs x 4 issue slots per clock x the sampled SM clock
   cpu_baseline  the oracle port (C restatement of the reference step, OpenMP on all host
              cores) on a bounded sample of the same workload
+  extras     batched_256 (the 256-scene mix, batched vs looped plain steps), dam_break_10M
+             (exact and precision mode, fresh-state), dam_break_1M_faithful (the workload's
+             own trajectory with per-step cell occupancy and non-finite counts, bounded to
+             30 s of device time)
 
 --impl reference times the reference's CPU implementation of the path (the oracle port:
 the reference's own build cannot be compiled on the GPU host) on all host cores, on the
@@ -56,7 +63,26 @@ FALLBACK_HBM_GBS = 6800.0
 
 def workload(name: str) -> I.Workload:
     return {"dam_break_10k": I.config0, "dam_break_1M": I.config1,
-            "dam_break_10M": I.config4}[name]()
+            "dam_break_10M": I.config4,
+            # 160^3 = 4.1M: the config-1 lattice large enough that its arrays exceed L2
+            # (the case the per-particle DRAM traffic of the passes is measured on)
+            "dam_break_4M": lambda: I.scaled_dam_break(160 ** 3, seed=1)}[name]()
+
+
+SM_COUNT_FALLBACK = 152
+ISSUE_PER_SM_PER_CLK = 4  # one warp instruction per clock per sub-partition, 4 per SM
+
+
+def ncu_issue(kernel: str):
+    """Warp instructions per particle of a pass (k_force / k_density) on the 1M dam break,
+    from the committed ncu summary; None if absent."""
+    p = REPO / "profiles" / "ncu_issue.json"
+    if not p.exists():
+        return None
+    try:
+        return float(json.loads(p.read_text())[kernel]["warp_inst_per_particle"])
+    except Exception:
+        return None
 
 
 def peaks() -> tuple[float, str]:
@@ -295,6 +321,46 @@ def bench_10m_precise(torch, stream, flush, w10, steps):
             "protocol": "fresh-state, CFL dt in FP64 (step(0)), captured graph"}
 
 
+def bench_faithful(torch, stream, w, budget_s=30.0):
+    """Faithful trajectory of the workload: its own step count and dt from the initial
+    state, each step timed on the device, with the grid's occupancy and the non-finite
+    count after every step.  The reference's dynamics pile the particles into the walls
+    within the first steps (the lattice starts at 2/3 of the rest density), after which a
+    step costs the square of the crowded cells' occupancy; the run stops after the step
+    that crosses `budget_s` of device time and reports the steps it did."""
+    import sphx
+
+    ctx = sphx.Context(w.n, profile=False)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_params(w.params)
+    ctx.upload(w.pos, w.vel, w.mass)
+    torch.cuda.synchronize()
+    log, total = [], 0.0
+    for s in range(w.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        ctx.step(w.dt)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        st = ctx.stats()
+        occ = max(st["occupied_cells"], 1)
+        log.append([round(ms, 3), st["occupied_cells"], st["max_cell_occupancy"],
+                    round(w.n / occ, 2), st["nonfinite_particles"]])
+        total += ms * 1e-3
+        if total > budget_s:
+            break
+    ctx.close()
+    done = len(log)
+    return {"value": w.n * done / total, "unit": UNIT, "steps_done": done, "steps": w.steps,
+            "dt": w.dt, "device_s": total, "ms_first_step": log[0][0], "ms_last_step": log[-1][0],
+            "per_step": log,
+            "per_step_fields": ["ms", "occupied_cells", "max_cell_occupancy",
+                                "mean_cell_occupancy", "nonfinite_particles"],
+            "protocol": f"faithful trajectory from the initial state, stopped after the step "
+                        f"crossing {budget_s:.0f} s of device time"}
+
+
 def bench_ours(args, world, rank, local):
     import torch
 
@@ -415,6 +481,10 @@ def bench_ours(args, world, rank, local):
         extra["dam_break_10M_precise"] = bench_10m_precise(torch, stream, flush, w10, k10)
     elif not ctx_closed(ctx):
         ctx.close()
+    if args.workload == "dam_break_1M" and not args.no_faithful:
+        if not ctx_closed(ctx):
+            ctx.close()
+        extra["dam_break_1M_faithful"] = bench_faithful(torch, stream, w)
 
     if rank != 0:
         if dist:
@@ -423,6 +493,23 @@ def bench_ours(args, world, rank, local):
 
     peak, peak_kind = peaks()
     achieved = FORCE_BYTES_PER_PARTICLE * w.n / force_s / 1e9
+    # the bound that applies: instruction issue (the passes do ~8 FP32 ops per candidate
+    # test and ~150 per exact pair term on L1/L2-resident data)
+    sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    sms = torch.cuda.get_device_properties(local).multi_processor_count or SM_COUNT_FALLBACK
+    issue_peak = sms * ISSUE_PER_SM_PER_CLK * sm_mhz * 1e6
+    issue = None
+    ipp = ncu_issue("k_force")
+    if ipp:
+        a_issue = ipp * w.n / force_s
+        issue = {"bound": "issue", "achieved": a_issue, "peak": issue_peak,
+                 "unit": "warp-inst/s", "frac": a_issue / issue_peak,
+                 "kernel": "k_force<true>",
+                 "source": "profiles/ncu_issue.json warp instructions per particle x particles "
+                           "/ CUDA-event kernel time; peak = SMs x 4 issue slots x median SM clock"}
+        ipd = ncu_issue("k_density")
+        if ipd:
+            issue["density_frac"] = ipd * w.n / dens_s / issue_peak
     traffic = ncu_traffic(args.workload, w.n)
     cpu = None
     if world == 1 and not args.no_cpu:
@@ -448,6 +535,7 @@ def bench_ours(args, world, rank, local):
                      "frac": achieved / peak, "traffic": traffic,
                      "kernel": "k_force<true> (force + leapfrog + clamp)",
                      "peak_source": f"{peak_kind} hbm_gbs"},
+        "roofline_issue": issue,
         "kernels_ms": {"grid_build": 1e3 * grid_s, "density": 1e3 * dens_s,
                        "force": 1e3 * force_s,
                        "density_hbm_frac": (DENSITY_BYTES_PER_PARTICLE * w.n / dens_s / 1e9) / peak},
@@ -471,10 +559,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--workload", default="dam_break_1M",
-                    choices=("dam_break_10k", "dam_break_1M", "dam_break_10M"))
+                    choices=("dam_break_10k", "dam_break_1M", "dam_break_4M", "dam_break_10M"))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-10m", action="store_true", help="skip the 10M secondary figures")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-scene figure")
+    ap.add_argument("--no-faithful", action="store_true",
+                    help="skip the faithful-trajectory figure")
     args = ap.parse_args()
     world, rank, local = dist_env()
     if args.impl == "reference":
