@@ -96,17 +96,18 @@ def peaks() -> tuple[float, str]:
 
 
 def ncu_traffic(workload_name: str, n: int):
-    """Per-launch DRAM bytes of the force kernel from the committed ncu summary, scaled
-    to this workload's particle count (traffic grows in proportion to particles)."""
+    """Per-launch DRAM bytes of the force kernel from the committed ncu summary (measured
+    per particle on the 4.1M lattice, whose arrays exceed L2), scaled to this workload's
+    particle count; returns (total, hit-mask records part) or (None, None)."""
     p = REPO / "profiles" / "ncu_traffic.json"
     if not p.exists():
-        return None
+        return None, None
     try:
         d = json.loads(p.read_text())
-        per = d["force"]["dram_bytes_per_particle"]
-        return float(per) * n
+        f = d["force"]
+        return float(f["dram_bytes_per_particle"]) * n, float(f["hit_mask_bytes_per_particle"]) * n
     except Exception:
-        return None
+        return None, None
 
 
 class ClockSampler:
@@ -510,7 +511,7 @@ def bench_ours(args, world, rank, local):
         ipd = ncu_issue("k_density")
         if ipd:
             issue["density_frac"] = ipd * w.n / dens_s / issue_peak
-    traffic = ncu_traffic(args.workload, w.n)
+    traffic, traffic_masks = ncu_traffic(args.workload, w.n)
     cpu = None
     if world == 1 and not args.no_cpu:
         cpu = run_cpu(w, steps=8, warmup=0, budget_s=15.0)
@@ -533,6 +534,10 @@ def bench_ours(args, world, rank, local):
                 "path": "sphx_upload (pinned) + sphx_step + sphx_download (pos, vel, rho)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
+                     "traffic_hit_masks": traffic_masks,
+                     "traffic_note": "DRAM bytes per launch = the particle data (about 1.3x the "
+                                     "72 B/particle algorithmic bytes) + the hit-mask records "
+                                     "the density pass wrote for this pass (read once)",
                      "kernel": "k_force<true> (force + leapfrog + clamp)",
                      "peak_source": f"{peak_kind} hbm_gbs"},
         "roofline_issue": issue,
