@@ -157,6 +157,24 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(dist, seconds: float, device: str = "cuda") -> float:
+    """The slowest rank's time: replicas finish when the last one does (no collective at
+    world size 1; NCCL on the GPUs, any backend's tensor device otherwise)."""
+    if dist is None:
+        return seconds
+    import torch
+
+    t = torch.tensor([seconds], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world: int, particles: int, steps: int, max_seconds: float) -> float:
+    """Whole-job particle-steps/s of `world` replicas each stepping `particles` `steps`
+    times, timed by the slowest."""
+    return world * particles * steps / max_seconds
+
+
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -406,12 +424,8 @@ def bench_ours(args, world, rank, local):
     clocks = sampler.stop() if sampler else None
     st = ctx.stats()
     launches = st["kernel_launches"] - launches0
-    dev_s = sum(ms) * 1e-3
-    if dist:
-        t = torch.tensor([dev_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_s = float(t.item())
-    value = world * w.n * args.steps / dev_s
+    dev_s = max_over_ranks(dist, sum(ms) * 1e-3)
+    value = replica_value(world, w.n, args.steps, dev_s)
     force_s = st["force_computation_time"] / args.steps
     dens_s = st["density_computation_time"] / args.steps
     grid_s = st["neighbor_search_time"] / args.steps
@@ -439,12 +453,8 @@ def bench_ours(args, world, rank, local):
         e2e_step()
     e1.record()
     torch.cuda.synchronize()
-    e2e_s = e0.elapsed_time(e1) * 1e-3
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * w.n * args.steps / e2e_s
+    e2e_s = max_over_ranks(dist, e0.elapsed_time(e1) * 1e-3)
+    e2e_value = replica_value(world, w.n, args.steps, e2e_s)
     # parity spot-check of the e2e output against the device path (same initial state)
     rho_e2e = o_rho.numpy().copy()
 
