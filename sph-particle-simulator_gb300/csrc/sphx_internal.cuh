@@ -241,16 +241,15 @@ __device__ __forceinline__ float cubic_grad_factor(const StepConst& c, float q) 
     return 0.0f;
 }
 
-// CubicSplineKernel::laplacianW_3d (kernels.cpp:130-138)
+// CubicSplineKernel::laplacianW_3d (kernels.cpp:130-138).  The branch picks the
+// numerator, one division follows: lanes of a warp hold q on both sides of 1, and a
+// division per branch would run twice.  Outside both ranges (and for NaN q) the numerator
+// is 0 and 0 / h_sq = +0, the reference's 0.0f.
 __device__ __forceinline__ float cubic_lap(const StepConst& c, float q) {
-    if (q >= 0.0f && q <= 1.0f) {
-        return xdiv_fixed(xmul(c.sigma, xadd(-2.0f, xmul(3.0f, q))), c.h_sq, c.rcp_hsq,
-                          c.fast_div_hsq);
-    } else if (q > 1.0f && q <= 2.0f) {
-        const float tmp = xsub(2.0f, q);
-        return xdiv_fixed(xmul(c.sigma, tmp), c.h_sq, c.rcp_hsq, c.fast_div_hsq);
-    }
-    return 0.0f;
+    const float a = (q > 1.0f) ? xsub(2.0f, q) : xadd(-2.0f, xmul(3.0f, q));
+    const bool in = (q >= 0.0f && q <= 1.0f) || (q > 1.0f && q <= 2.0f);
+    const float num = in ? xmul(c.sigma, a) : 0.0f;
+    return xdiv_fixed(num, c.h_sq, c.rcp_hsq, c.fast_div_hsq);
 }
 
 // WendlandC2Kernel::W after q = length(r)/h (kernels.cpp:172-178):

@@ -291,6 +291,23 @@ __device__ __forceinline__ uint32_t warp_excl_scan(uint32_t v, int lane, uint32_
     return x - v;
 }
 
+// Writes this lane's hits (mask) to plist[o, o + popc(mask)) as (lane << 5) | candidate,
+// in candidate order, two per iteration.
+__device__ __forceinline__ void list_hits(uint16_t* plist, uint32_t mask, uint32_t o, int lane) {
+    const uint32_t tag = (uint32_t)lane << 5;
+    uint32_t mm = mask, k = o;
+    while (mm) {
+        const uint32_t a = __ffs(mm) - 1;
+        mm &= mm - 1;
+        plist[k] = (uint16_t)(tag | a);
+        if (!mm) break;
+        const uint32_t b = __ffs(mm) - 1;
+        mm &= mm - 1;
+        plist[k + 1] = (uint16_t)(tag | b);
+        k += 2;
+    }
+}
+
 // Axis-aligned box of the tile's particles (valid lanes).
 struct TileBox {
     float lo[3], hi[3];
@@ -484,8 +501,7 @@ __global__ void __launch_bounds__(128, 8) k_density(const StepConst cp, const Bu
                 uint32_t H;
                 const uint32_t o = warp_excl_scan(cnt, lane, H);
                 if (!H) continue;
-                for (uint32_t mm = mask, k = o; mm; mm &= mm - 1, ++k)
-                    S->plist[k] = (uint16_t)((lane << 5) | (__ffs(mm) - 1));
+                list_hits(S->plist, mask, o, lane);
                 __syncwarp();
                 for (uint32_t base = 0; base < H; base += kDensityBatch) {
                     const uint32_t end = min(H, base + kDensityBatch);
@@ -539,8 +555,7 @@ struct ForceSmem {
     float4 box_lo, box_hi;  // tile box (the fallback walk's culling test)
     int2 seg[kMaxSegments]; // the tile's row segments
     float4 cpos[32], cvel[32], caux[32];
-    float4 tpos[32], tvel[32];
-    float tP[32];
+    float4 tpos[32], tvel[32];  // targets: x,y,z,m and vx,vy,vz,P
     uint16_t plist[32 * 32];
     float4 tbA[kForceBatch];  // pressure term x, y, z and viscosity term x
     float2 tbB[kForceBatch];  // viscosity term y, z
@@ -733,12 +748,13 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buff
             }
         }
         S->tpos[lane] = xi;
-        S->tvel[lane] = vi0;
-        S->tP[lane] = Pi;
+        S->tvel[lane] = make_float4(vi0.x, vi0.y, vi0.z, Pi);
         float fpx = 0.0f, fpy = 0.0f, fpz = 0.0f;
         float fvx = 0.0f, fvy = 0.0f, fvz = 0.0f;
         KSum Fx, Fy, Fz;  // precision mode: one compensated sum per component
         const uint32_t* rec = slot != kNoSlot ? b.hitmask + (size_t)slot * 32 + lane : nullptr;
+        uint32_t mnext =
+            rec && (size_t)(rec - b.hitmask) < (size_t)b.hitmask_cap * 32 ? __ldcs(rec) : 0u;
         const int nseg = build_segments(b, g, T, lane, S->seg);
         __syncwarp();
         for (int sg = 0; sg < nseg; ++sg) {
@@ -749,7 +765,11 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buff
                 uint32_t mask;
                 __syncwarp();
                 if (rec) {
-                    mask = __ldcs(rec);  // read once
+                    mask = mnext;
+                    // the next chunk's record, loaded a chunk ahead (past the tile's last
+                    // chunk it reads another tile's record, or nothing at the pool's end)
+                    mnext = (size_t)(rec + 32 - b.hitmask) < (size_t)b.hitmask_cap * 32
+                                ? __ldcs(rec + 32) : 0u;
                     const uint32_t used = __reduce_or_sync(kFull, mask);  // candidates hit
                     if (!used) continue;
                     if (used & (1u << lane)) {
@@ -785,8 +805,7 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buff
                 uint32_t H;
                 const uint32_t o = warp_excl_scan(cnt, lane, H);
                 if (!H) continue;
-                for (uint32_t mm = mask, k = o; mm; mm &= mm - 1, ++k)
-                    S->plist[k] = (uint16_t)((lane << 5) | (__ffs(mm) - 1));
+                list_hits(S->plist, mask, o, lane);
                 __syncwarp();
                 for (uint32_t base = 0; base < H; base += kForceBatch) {
                     const uint32_t end = min(H, base + kForceBatch);
@@ -794,12 +813,13 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buff
                         const uint32_t pr = S->plist[f];
                         const int tt = pr >> 5, jj = pr & 31;
                         float p3[3], v3[3];
+                        const float4 vt = S->tvel[tt];
                         if (kPrecise)
-                            force_term_p<kKern>(c, S->tpos[tt], S->tvel[tt], S->tP[tt],
-                                                S->cpos[jj], S->cvel[jj], S->caux[jj], p3, v3);
+                            force_term_p<kKern>(c, S->tpos[tt], vt, vt.w, S->cpos[jj],
+                                                S->cvel[jj], S->caux[jj], p3, v3);
                         else
-                            force_term<kKern>(c, S->tpos[tt], S->tvel[tt], S->tP[tt],
-                                              S->cpos[jj], S->cvel[jj], S->caux[jj], p3, v3);
+                            force_term<kKern>(c, S->tpos[tt], vt, vt.w, S->cpos[jj],
+                                              S->cvel[jj], S->caux[jj], p3, v3);
                         const uint32_t u = f - base;
                         S->tbA[u] = make_float4(p3[0], p3[1], p3[2], v3[0]);
                         S->tbB[u] = make_float2(v3[1], v3[2]);
