@@ -207,6 +207,35 @@ __device__ __forceinline__ float xdiv_fixed(float a, float b, float y, int verif
     return __fdiv_rn(a, b);
 }
 
+// Packed FP32 pairs (Blackwell f32x2 instructions): two IEEE round-to-nearest operations in
+// one instruction, each element rounded exactly as the scalar __f*_rn would.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float a, float b) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float2 upk2(f32x2 v) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+__device__ __forceinline__ f32x2 xsub2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 xmul2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 xadd2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
 // glm::dot(v, v) = (x*x + y*y) + z*z (products rounded first)
 __device__ __forceinline__ float xdot3(float x, float y, float z) {
     return xadd(xadd(xmul(x, x), xmul(y, y)), xmul(z, z));

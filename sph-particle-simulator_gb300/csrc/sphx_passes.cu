@@ -364,6 +364,29 @@ __device__ __forceinline__ uint32_t chunk_hits(const float4* cand, uint32_t surv
     return mask;
 }
 
+// chunk_hits<false> two candidates at a time with packed FP32 pairs: the same exact test
+// (x_i - x_j per axis, (dx*dx + dy*dy) + dz*dz, <= r^2), element by element.  Candidates
+// outside `surv` are farther than r from every lane (the box cull is conservative), so a
+// pair is skipped only when both of its candidates are.
+__device__ __forceinline__ uint32_t chunk_hits_x2(const float* cx, const float* cy,
+                                                  const float* cz, uint32_t surv,
+                                                  const float4& xi, float r2) {
+    const f32x2 X = pk2(xi.x, xi.x), Y = pk2(xi.y, xi.y), Z = pk2(xi.z, xi.z);
+    uint32_t mask = 0;
+#pragma unroll
+    for (int jj = 0; jj < 32; jj += 2) {
+        if ((surv >> jj) & 3u) {
+            const f32x2 dx = xsub2(X, *reinterpret_cast<const f32x2*>(cx + jj));
+            const f32x2 dy = xsub2(Y, *reinterpret_cast<const f32x2*>(cy + jj));
+            const f32x2 dz = xsub2(Z, *reinterpret_cast<const f32x2*>(cz + jj));
+            const float2 d2 = upk2(xadd2(xadd2(xmul2(dx, dx), xmul2(dy, dy)), xmul2(dz, dz)));
+            if (d2.x <= r2) mask |= 1u << jj;
+            if (d2.y <= r2) mask |= 2u << jj;
+        }
+    }
+    return mask;
+}
+
 // W(q) in precision mode (same formula, contracted arithmetic)
 __device__ __forceinline__ float cubic_w_p(const StepConst& c, float q) {
     if (q <= 1.0f) return c.sigma * (2.0f / 3.0f - q * q + 0.5f * q * q * q);
@@ -413,6 +436,9 @@ struct DensitySmem {
     uint32_t mcur, mend;    // the warp's region of the hit-mask pool: [mcur, mend)
     int2 seg[kMaxSegments]; // the tile's row segments
     float4 cand[32];
+    __align__(8) float cx[32];  // the candidates' coordinates again, as arrays: the exact
+    __align__(8) float cy[32];  // test reads two candidates' x (y, z) in one 64-bit load
+    __align__(8) float cz[32];
     float4 tpos[32];
     uint16_t plist[32 * 32];
     float tbuf[kDensityBatch];
@@ -477,6 +503,11 @@ __global__ void __launch_bounds__(128, 8) k_density(const StepConst cp, const Bu
                 float4 pl = lane < m ? b.pos4_s[s + lane] : make_float4(inf, inf, inf, 0.f);
                 if (kPrecise && lane < m) pl = frame_pos(b.cell4_s[s + lane], frame, pl, c.cs);
                 S->cand[lane] = pl;
+                if (!kPrecise) {
+                    S->cx[lane] = pl.x;
+                    S->cy[lane] = pl.y;
+                    S->cz[lane] = pl.z;
+                }
                 TileBox B;
                 {
                     const float4 lo = S->box_lo, hi = S->box_hi;
@@ -492,7 +523,9 @@ __global__ void __launch_bounds__(128, 8) k_density(const StepConst cp, const Bu
                     if (rec) __stcs(rec, 0u);
                     continue;
                 }
-                uint32_t mask = valid ? chunk_hits<kPrecise>(S->cand, surv, xi, c.r2) : 0u;
+                uint32_t mask = 0u;
+                if (valid) mask = kPrecise ? chunk_hits<true>(S->cand, surv, xi, c.r2)
+                                           : chunk_hits_x2(S->cx, S->cy, S->cz, surv, xi, c.r2);
                 if (rec) __stcs(rec, mask);
                 nn += __popc(mask);
                 const int self = i - s;
