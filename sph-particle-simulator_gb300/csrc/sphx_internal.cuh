@@ -236,6 +236,27 @@ __device__ __forceinline__ f32x2 xadd2(f32x2 a, f32x2 b) {
     return d;
 }
 
+__device__ __forceinline__ f32x2 xfma2(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// xdiv_fixed of a pair of dividends: the one-correction sequence with packed FP32 pairs
+// when both dividends are in its range (-b is passed pre-negated: fma(q0, -b, a) is the
+// exact a - q0 b), else element by element.
+__device__ __forceinline__ f32x2 xdiv_fixed2(f32x2 a2, float b, float y, int verified) {
+    const float2 a = upk2(a2);
+    const float ax = fabsf(a.x), ay = fabsf(a.y);
+    if (verified && ax >= 0x1p-60f && ax <= 0x1p60f && ay >= 0x1p-60f && ay <= 0x1p60f) {
+        const f32x2 y2 = pk2(y, y);
+        const f32x2 q0 = xmul2(a2, y2);
+        const f32x2 r = xfma2(q0, pk2(-b, -b), a2);
+        return xfma2(r, y2, q0);
+    }
+    return pk2(xdiv_fixed(a.x, b, y, verified), xdiv_fixed(a.y, b, y, verified));
+}
+
 // glm::dot(v, v) = (x*x + y*y) + z*z (products rounded first)
 __device__ __forceinline__ float xdot3(float x, float y, float z) {
     return xadd(xadd(xmul(x, x), xmul(y, y)), xmul(z, z));

@@ -590,8 +590,8 @@ struct ForceSmem {
     float4 cpos[32], cvel[32], caux[32];
     float4 tpos[32], tvel[32];  // targets: x,y,z,m and vx,vy,vz,P
     uint16_t plist[32 * 32];
-    float4 tbA[kForceBatch];  // pressure term x, y, z and viscosity term x
-    float2 tbB[kForceBatch];  // viscosity term y, z
+    float4 tbA[kForceBatch];  // pressure term x, y and viscosity term x, y
+    float2 tbB[kForceBatch];  // pressure term z, viscosity term z
 };
 
 // The pair term of particle t against candidate j: the pressure-force contribution
@@ -662,6 +662,44 @@ __device__ __forceinline__ void force_term(const StepConst& c, const float4& xt,
     v3[0] = xmul(xmul(sv, xsub(vj.x, vt.x)), lap);
     v3[1] = xmul(xmul(sv, xsub(vj.y, vt.y)), lap);
     v3[2] = xmul(xmul(sv, xsub(vj.z, vt.z)), lap);
+}
+
+// force_term<CUBIC_SPLINE> with the x and y components of every component-wise step done
+// as packed FP32 pairs (same operations, same rounding, element by element); returns the
+// record (p.x, p.y, v.x, v.y), (p.z, v.z).
+__device__ __forceinline__ void force_term_cubic_x2(const StepConst& c, const float4& xt,
+                                                    const float4& vt, float Pt,
+                                                    const float4& xj, const float4& vj,
+                                                    const float4& aj, float4& A, float2& B) {
+    const f32x2 dxy = xsub2(pk2(xt.x, xt.y), pk2(xj.x, xj.y));
+    const float dz = xsub(xt.z, xj.z);
+    const float2 sq = upk2(xmul2(dxy, dxy));
+    const float r_len = xsqrt(xadd(xadd(sq.x, sq.y), xmul(dz, dz)));
+    const float q = xdiv_fixed(r_len, c.h, c.rcp_h, c.fast_div_h);
+    f32x2 pxy = pk2(0.0f, 0.0f);
+    float pz = 0.0f;
+    if (!(r_len < 1e-6f)) {
+        const float pt = xdiv(xadd(Pt, aj.y), aj.z);
+        const float sp = xmul(xj.w, pt);
+        f32x2 gxy = pk2(0.0f, 0.0f);
+        float gz = 0.0f;
+        if ((q >= 0.0f && q <= 1.0f) || (q > 1.0f && q <= 2.0f)) {
+            const float gf = cubic_grad_factor(c, q);
+            const float2 d = upk2(dxy);
+            gxy = xmul2(pk2(gf, gf), pk2(xdiv(d.x, r_len), xdiv(d.y, r_len)));
+            gz = xmul(gf, xdiv(dz, r_len));
+        }
+        pxy = xmul2(pk2(sp, sp), xdiv_fixed2(gxy, c.h, c.rcp_h, c.fast_div_h));
+        pz = xmul(sp, xdiv_fixed(gz, c.h, c.rcp_h, c.fast_div_h));
+    }
+    const float lap = cubic_lap(c, q);
+    const float sv = xmul(aj.w, c.visc);
+    const f32x2 vxy = xmul2(xmul2(pk2(sv, sv), xsub2(pk2(vj.x, vj.y), pk2(vt.x, vt.y))),
+                            pk2(lap, lap));
+    const float vz = xmul(xmul(sv, xsub(vj.z, vt.z)), lap);
+    const float2 p = upk2(pxy), v = upk2(vxy);
+    A = make_float4(p.x, p.y, v.x, v.y);
+    B = make_float2(pz, vz);
 }
 
 // Precision-mode pair term: the same formulas with contracted FP32 arithmetic.
@@ -782,8 +820,8 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buff
         }
         S->tpos[lane] = xi;
         S->tvel[lane] = make_float4(vi0.x, vi0.y, vi0.z, Pi);
-        float fpx = 0.0f, fpy = 0.0f, fpz = 0.0f;
-        float fvx = 0.0f, fvy = 0.0f, fvz = 0.0f;
+        f32x2 fpxy = pk2(0.0f, 0.0f), fvxy = pk2(0.0f, 0.0f);  // (x, y) sums, packed
+        float fpz = 0.0f, fvz = 0.0f;
         KSum Fx, Fy, Fz;  // precision mode: one compensated sum per component
         const uint32_t* rec = slot != kNoSlot ? b.hitmask + (size_t)slot * 32 + lane : nullptr;
         uint32_t mnext =
@@ -847,15 +885,24 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buff
                         const int tt = pr >> 5, jj = pr & 31;
                         float p3[3], v3[3];
                         const float4 vt = S->tvel[tt];
+                        const uint32_t u = f - base;
+                        if (!kPrecise && kKern == SPHX_KERNEL_CUBIC_SPLINE) {
+                            float4 A;
+                            float2 Bp;
+                            force_term_cubic_x2(c, S->tpos[tt], vt, vt.w, S->cpos[jj],
+                                                S->cvel[jj], S->caux[jj], A, Bp);
+                            S->tbA[u] = A;
+                            S->tbB[u] = Bp;
+                            continue;
+                        }
                         if (kPrecise)
                             force_term_p<kKern>(c, S->tpos[tt], vt, vt.w, S->cpos[jj],
                                                 S->cvel[jj], S->caux[jj], p3, v3);
                         else
                             force_term<kKern>(c, S->tpos[tt], vt, vt.w, S->cpos[jj],
                                               S->cvel[jj], S->caux[jj], p3, v3);
-                        const uint32_t u = f - base;
-                        S->tbA[u] = make_float4(p3[0], p3[1], p3[2], v3[0]);
-                        S->tbB[u] = make_float2(v3[1], v3[2]);
+                        S->tbA[u] = make_float4(p3[0], p3[1], v3[0], v3[1]);
+                        S->tbB[u] = make_float2(p3[2], v3[2]);
                     }
                     __syncwarp();
                     const uint32_t k1 = min(o + cnt, end);
@@ -864,17 +911,15 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buff
                         const float4 A = S->tbA[u];
                         const float2 Bv = S->tbB[u];
                         if (kPrecise) {
-                            Fx.add(A.w - A.x);
-                            Fy.add(Bv.x - A.y);
-                            Fz.add(Bv.y - A.z);
+                            Fx.add(A.z - A.x);
+                            Fy.add(A.w - A.y);
+                            Fz.add(Bv.y - Bv.x);
                             continue;
                         }
                         // a skipped pressure term is +0, and x - (+0) == x exactly
-                        fpx = xsub(fpx, A.x);
-                        fpy = xsub(fpy, A.y);
-                        fpz = xsub(fpz, A.z);
-                        fvx = xadd(fvx, A.w);
-                        fvy = xadd(fvy, Bv.x);
+                        fpxy = xsub2(fpxy, pk2(A.x, A.y));
+                        fvxy = xadd2(fvxy, pk2(A.z, A.w));
+                        fpz = xsub(fpz, Bv.x);
                         fvz = xadd(fvz, Bv.y);
                     }
                     __syncwarp();
@@ -890,8 +935,9 @@ __global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buff
             ay = (Fy.value() + c.grav * mi) / mi;
             az = Fz.value() / mi;
         } else {
-            ax = xdiv(xadd(xadd(fpx, fvx), xmul(0.0f, mi)), mi);
-            ay = xdiv(xadd(xadd(fpy, fvy), xmul(c.grav, mi)), mi);
+            const float2 fp = upk2(fpxy), fv = upk2(fvxy);
+            ax = xdiv(xadd(xadd(fp.x, fv.x), xmul(0.0f, mi)), mi);
+            ay = xdiv(xadd(xadd(fp.y, fv.y), xmul(c.grav, mi)), mi);
             az = xdiv(xadd(xadd(fpz, fvz), xmul(0.0f, mi)), mi);
         }
         b.acc4_s[i] = make_float4(ax, ay, az, 0.0f);
