@@ -146,7 +146,10 @@ int sphx_get_kernel(sphx_ctx* ctx, int* kernel);
  * SPHEngine::add_particles / clear_particles, src/sph_engine.cpp:83-91).  vel may be NULL
  * (zero).  n > capacity -> SPHX_ERR_CAPACITY (the host engine applies the reference's
  * drop-with-warning rule before calling).  The acceleration used by the CFL rule for
- * particle 0 persists across uploads, as the reference's accelerations_ buffer does. */
+ * particle 0 persists across uploads, as the reference's accelerations_ buffer does.
+ * Pinned host buffers (cudaHostAlloc / cudaHostRegister) are read in place by the GPU,
+ * over the coherent CPU-GPU link, when the stream reaches the call: keep them unchanged
+ * until then.  Pageable buffers are copied before the call returns. */
 int sphx_upload(sphx_ctx* ctx, size_t n, const float* pos_xyz, const float* vel_xyz,
                 const float* mass);
 
@@ -164,7 +167,8 @@ int sphx_eval(sphx_ctx* ctx);
 /* Copies fields of the current state to host memory in insertion order; synchronises.
  * SPHEngine::get_positions / get_velocities / get_densities / get_pressures
  * (src/sph_engine.h:133-136).  Any pointer may be NULL.  rho/p/acc are those of the last
- * step or eval (acc is the reference's accelerations_ buffer). */
+ * step or eval (acc is the reference's accelerations_ buffer).  Returns the step's device
+ * status (SPHX_OK, or the error a kernel recorded). */
 int sphx_download(sphx_ctx* ctx, float* pos_xyz, float* vel_xyz, float* rho, float* pressure,
                   float* acc_xyz);
 

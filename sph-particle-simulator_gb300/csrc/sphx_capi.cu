@@ -28,7 +28,7 @@ struct sphx_ctx {
     Buffers b{};
     int kernel = SPHX_KERNEL_CUBIC_SPLINE;
     DevState* ds = nullptr;
-    float* stage = nullptr;    // 10 * capacity floats (room for FP64 positions)
+    float* stage = nullptr;    // 11 * capacity floats (FP64 positions; all download fields)
     float4* snap_pos = nullptr;
     float4* snap_vel = nullptr;
     int4* snap_cell = nullptr;
@@ -59,6 +59,10 @@ struct sphx_ctx {
     unsigned long long* r_keys = nullptr;
     uchar4* r_rgba = nullptr;
     size_t r_pix_cap = 0;
+    int* h_status = nullptr;  // pinned host word: the device status, read with the results
+    // second stream for device-to-host copies that can run beside the main stream's
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_unpacked = nullptr, ev_copied = nullptr;
     static constexpr int kProfRing = 64;
     struct ProfSlot {
         cudaEvent_t ev[5];
@@ -223,6 +227,10 @@ void free_all(sphx_ctx* c) {
     for (auto& slot : c->prof)
         for (auto& e : slot.ev)
             if (e) cudaEventDestroy(e);
+    if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->ev_unpacked) cudaEventDestroy(c->ev_unpacked);
+    if (c->ev_copied) cudaEventDestroy(c->ev_copied);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
 }
@@ -249,12 +257,13 @@ int drain_all(sphx_ctx* c) {
     return SPHX_OK;
 }
 
+// Waits for the context's stream and returns the device status word (read on the stream,
+// into pinned memory, so other streams are not waited for).
 int sync_status(sphx_ctx* c) {
+    SPHX_CUDA(cudaMemcpyAsync(c->h_status, c->ds, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     SPHX_CUDA(cudaStreamSynchronize(c->stream));
     SPHX_CUDA(cudaGetLastError());
-    int st[2] = {0, 0};
-    SPHX_CUDA(cudaMemcpy(st, c->ds, sizeof(int), cudaMemcpyDeviceToHost));
-    return st[0];
+    return *c->h_status;
 }
 
 int enter(sphx_ctx* c) {
@@ -344,6 +353,21 @@ int run_step_graph(sphx_ctx* c, float dt) {
     return SPHX_OK;
 }
 
+
+// Device address of a host buffer the GPU can access in place (pinned: cudaHostAlloc or
+// cudaHostRegister), or null (pageable memory: the caller's data go through staging).
+// On Grace + Blackwell the kernels then read and write it over the coherent C2C link.
+template <class T>
+T* mapped(T* h) {
+    if (!h) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return (a.type == cudaMemoryTypeHost && a.devicePointer) ? static_cast<T*>(a.devicePointer)
+                                                             : nullptr;
+}
 
 // ---- headless rendering helpers ----------------------------------------------------------
 
@@ -590,7 +614,7 @@ int sphx_create(sphx_ctx** out, size_t capacity, const sphx_tuning* tuning) {
         (rc = dmalloc(&b.tile_start, C)) || (rc = dmalloc(&b.hist, hist_n)) ||
         (rc = dmalloc(&b.scan_part, (size_t)b.scan_part_cap)) ||
         (rc = dmalloc(&b.diag_part, (size_t)b.diag_blocks * kDiagSums)) ||
-        (rc = dmalloc(&c->ds, 1)) || (rc = dmalloc(&c->stage, 10 * C)))
+        (rc = dmalloc(&c->ds, 1)) || (rc = dmalloc(&c->stage, 11 * C)))
         return fail(rc);
     if (c->tuning.mode != SPHX_MODE_EXACT &&
         ((rc = dmalloc(&b.cell4, C)) || (rc = dmalloc(&b.cell4_s, C))))
@@ -613,6 +637,16 @@ int sphx_create(sphx_ctx** out, size_t capacity, const sphx_tuning* tuning) {
         cudaGetLastError();
     }
     if (cudaMemset(c->ds, 0, sizeof(DevState)) != cudaSuccess) return fail(SPHX_ERR_CUDA);
+    if (cudaHostAlloc(reinterpret_cast<void**>(&c->h_status), sizeof(int), cudaHostAllocDefault) !=
+        cudaSuccess) {
+        c->h_status = nullptr;
+        return fail(SPHX_ERR_OOM);
+    }
+    *c->h_status = 0;
+    if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_unpacked, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_copied, cudaEventDisableTiming) != cudaSuccess)
+        return fail(SPHX_ERR_CUDA);
     if (cudaMemset(b.aux4_s, 0, C * sizeof(float4)) != cudaSuccess ||
         cudaMemset(b.acc4_s, 0, C * sizeof(float4)) != cudaSuccess)
         return fail(SPHX_ERR_CUDA);
@@ -710,10 +744,18 @@ int sphx_upload(sphx_ctx* c, size_t n, const float* pos, const float* vel, const
     float* s_vel = c->stage + 3 * c->capacity;
     float* s_mass = c->stage + 6 * c->capacity;
     if (n > 0) {
-        SPHX_CUDA(cudaMemcpyAsync(s_pos, pos, 3 * n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-        if (vel)
-            SPHX_CUDA(cudaMemcpyAsync(s_vel, vel, 3 * n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-        SPHX_CUDA(cudaMemcpyAsync(s_mass, mass, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+        // pinned host buffers are read in place by the pack kernel; others are staged
+        const float* m_pos = mapped(pos);
+        const float* m_vel = mapped(vel);
+        const float* m_mass = mapped(mass);
+        if (m_pos) s_pos = const_cast<float*>(m_pos);
+        else SPHX_CUDA(cudaMemcpyAsync(s_pos, pos, 3 * n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+        if (vel) {
+            if (m_vel) s_vel = const_cast<float*>(m_vel);
+            else SPHX_CUDA(cudaMemcpyAsync(s_vel, vel, 3 * n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+        }
+        if (m_mass) s_mass = const_cast<float*>(m_mass);
+        else SPHX_CUDA(cudaMemcpyAsync(s_mass, mass, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
         if (c->b.cell4) {
             fill_step_const(c);
             launch_pack_cells(c->L, c->sc, (int)n, s_pos, nullptr, vel ? s_vel : nullptr, s_mass,
@@ -958,15 +1000,22 @@ int sphx_eval(sphx_ctx* c) {
     return run_phases(c, 0.0f, false);
 }
 
+// Every unpack and copy is enqueued behind the pending work, with the device status word;
+// one synchronisation at the end.  Staging (11 floats per particle of capacity C): pos at
+// [0, 3C), vel at [3C, 6C), rho at [6C, 7C), P at [7C, 8C), acc at [8C, 11C).
 int sphx_download(sphx_ctx* c, float* pos, float* vel, float* rho, float* pressure, float* acc) {
     int rc = enter(c);
     if (rc) return rc;
-    rc = sync_status(c);
-    if (rc) return rc;
     const size_t n = c->n;
-    if (n == 0) return SPHX_OK;
+    if (n == 0) return sync_status(c);
+    // outputs go through device staging and the copy engines (on Grace + Blackwell the
+    // copy engines write host memory faster than kernel stores over the C2C link do); the
+    // copies are split over two streams so that two copy engines run at once
     float* s0 = c->stage;
     float* s1 = c->stage + 3 * c->capacity;
+    float* s_rho = c->stage + 6 * c->capacity;
+    float* s_p = c->stage + 7 * c->capacity;
+    float* s_acc = c->stage + 8 * c->capacity;
     if (pos || vel) {
         launch_unpack_state(c->L, (int)n, c->b.pos4, c->b.vel4,
                             (pos && !c->b.cell4) ? s0 : nullptr, vel ? s1 : nullptr);
@@ -975,28 +1024,31 @@ int sphx_download(sphx_ctx* c, float* pos, float* vel, float* rho, float* pressu
             launch_unpack_cells(c->L, c->sc, (int)n, c->b.cell4, c->b.pos4, s0, nullptr);
         }
         SPHX_CUDA(cudaGetLastError());
-        if (pos) SPHX_CUDA(cudaMemcpyAsync(pos, s0, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
-        if (vel) SPHX_CUDA(cudaMemcpyAsync(vel, s1, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
-        SPHX_CUDA(cudaStreamSynchronize(c->stream));
     }
     if (rho || pressure || acc) {
-        float* s_rho = c->stage;
-        float* s_p = c->stage + c->capacity;
-        float* s_acc = c->stage + 2 * c->capacity;
         if (c->have_fields) {
             launch_unpack_sorted(c->L, (int)n, c->b.id_s, c->b.aux4_s, c->b.acc4_s,
                                  rho ? s_rho : nullptr, pressure ? s_p : nullptr,
                                  acc ? s_acc : nullptr);
             SPHX_CUDA(cudaGetLastError());
         } else {
-            SPHX_CUDA(cudaMemsetAsync(c->stage, 0, 5 * n * sizeof(float), c->stream));
+            SPHX_CUDA(cudaMemsetAsync(s_rho, 0, 5 * c->capacity * sizeof(float), c->stream));
         }
-        if (rho) SPHX_CUDA(cudaMemcpyAsync(rho, s_rho, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
-        if (pressure) SPHX_CUDA(cudaMemcpyAsync(pressure, s_p, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
-        if (acc) SPHX_CUDA(cudaMemcpyAsync(acc, s_acc, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
-        SPHX_CUDA(cudaStreamSynchronize(c->stream));
     }
-    return SPHX_OK;
+    SPHX_CUDA(cudaEventRecord(c->ev_unpacked, c->stream));
+    SPHX_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_unpacked, 0));
+    const size_t f = sizeof(float);
+    if (pos) SPHX_CUDA(cudaMemcpyAsync(pos, s0, 3 * n * f, cudaMemcpyDeviceToHost, c->stream));
+    if (vel) SPHX_CUDA(cudaMemcpyAsync(vel, s1, 3 * n * f, cudaMemcpyDeviceToHost, c->copy_stream));
+    if (rho) SPHX_CUDA(cudaMemcpyAsync(rho, s_rho, n * f, cudaMemcpyDeviceToHost, c->stream));
+    if (pressure) SPHX_CUDA(cudaMemcpyAsync(pressure, s_p, n * f, cudaMemcpyDeviceToHost, c->copy_stream));
+    if (acc) SPHX_CUDA(cudaMemcpyAsync(acc, s_acc, 3 * n * f, cudaMemcpyDeviceToHost, c->copy_stream));
+    SPHX_CUDA(cudaEventRecord(c->ev_copied, c->copy_stream));
+    SPHX_CUDA(cudaStreamWaitEvent(c->stream, c->ev_copied, 0));
+    SPHX_CUDA(cudaMemcpyAsync(c->h_status, c->ds, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    SPHX_CUDA(cudaStreamSynchronize(c->stream));
+    SPHX_CUDA(cudaGetLastError());
+    return *c->h_status;  // a failed step's outputs are not to be used
 }
 
 int sphx_download_f64(sphx_ctx* c, double* pos_xyz) {
