@@ -278,7 +278,7 @@ __device__ __forceinline__ Diff diff(const float4& xi, const float4& xj) {
 
 constexpr uint32_t kFull = 0xffffffffu;
 constexpr int kDensityBatch = 256;  // flattened terms computed per round (density)
-constexpr int kForceBatch = 128;    // flattened terms computed per round (force)
+constexpr int kForceBatch = 96;     // flattened terms computed per round (force)
 
 __device__ __forceinline__ uint32_t warp_excl_scan(uint32_t v, int lane, uint32_t& total) {
     uint32_t x = v;
@@ -786,7 +786,7 @@ __device__ __forceinline__ void integrate_cells(const StepConst& c, float dt, co
 }
 
 template <bool kIntegrate, bool kPrecise, bool kBatch, int kKern>
-__global__ void __launch_bounds__(128, 6) k_force(const StepConst cp, const Buffers b,
+__global__ void __launch_bounds__(128, 7) k_force(const StepConst cp, const Buffers b,
                                                DevState* ds) {
     if (ds->status) return;
     extern __shared__ __align__(16) unsigned char smem_raw_f[];
