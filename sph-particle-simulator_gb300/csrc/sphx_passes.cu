@@ -445,7 +445,7 @@ struct DensitySmem {
 };
 
 template <bool kPrecise, bool kBatch, int kKern>
-__global__ void __launch_bounds__(128, 8) k_density(const StepConst cp, const Buffers b,
+__global__ void __launch_bounds__(128, 10) k_density(const StepConst cp, const Buffers b,
                                                  DevState* ds) {
     if (ds->status) return;
     extern __shared__ __align__(16) unsigned char smem_raw_d[];
@@ -1072,8 +1072,8 @@ static void launch_density_t(const LaunchCtx& L, const StepConst& c, const Buffe
                              DevState* ds) {
     const int threads = 32 * L.warps_per_block;
     const size_t sm = (size_t)L.warps_per_block * sizeof(DensitySmem);
-    static int blocks[5][8] = {};
-    int& nb = blocks[L.warps_per_block][L.blocks_per_sm & 7];
+    static int blocks[5][33] = {};  // by warps per block, requested CTAs per SM (<= 32)
+    int& nb = blocks[L.warps_per_block][L.blocks_per_sm < 32 ? L.blocks_per_sm : 32];
     if (!nb) nb = resident_blocks(L, k_density<kPrecise, kBatch, kKern>, threads, sm);
     k_density<kPrecise, kBatch, kKern><<<nb, threads, sm, L.stream>>>(c, b, ds);
 }
@@ -1098,8 +1098,8 @@ static void launch_force_t(const LaunchCtx& L, const StepConst& c, const Buffers
                            DevState* ds) {
     const int threads = 32 * L.warps_per_block;
     const size_t sm = (size_t)L.warps_per_block * sizeof(ForceSmem);
-    static int blocks[5][8] = {};
-    int& nb = blocks[L.warps_per_block][L.blocks_per_sm & 7];
+    static int blocks[5][33] = {};  // by warps per block, requested CTAs per SM (<= 32)
+    int& nb = blocks[L.warps_per_block][L.blocks_per_sm < 32 ? L.blocks_per_sm : 32];
     if (!nb) nb = resident_blocks(L, k_force<kIntegrate, kPrecise, kBatch, kKern>, threads, sm);
     k_force<kIntegrate, kPrecise, kBatch, kKern><<<nb, threads, sm, L.stream>>>(c, b, ds);
 }
