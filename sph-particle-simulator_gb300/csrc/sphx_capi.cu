@@ -765,11 +765,13 @@ int sphx_upload(sphx_ctx* c, size_t n, const float* pos, const float* vel, const
         }
         SPHX_CUDA(cudaGetLastError());
     }
+    // a captured step graph stays valid for a new particle set of the same size (same
+    // buffers, same launch parameters); a size change or dropped scenes invalidate it
+    if (n != c->n || c->nscenes) c->version++;
     c->n = n;
     c->have_fields = false;
     c->b.nscenes = 0;  // a new particle set: scenes must be set again
     c->nscenes = 0;
-    c->version++;
     return SPHX_OK;
 }
 
@@ -804,11 +806,13 @@ int sphx_upload_f64(sphx_ctx* c, size_t n, const double* pos, const float* vel,
         }
         SPHX_CUDA(cudaGetLastError());
     }
+    // a captured step graph stays valid for a new particle set of the same size (same
+    // buffers, same launch parameters); a size change or dropped scenes invalidate it
+    if (n != c->n || c->nscenes) c->version++;
     c->n = n;
     c->have_fields = false;
     c->b.nscenes = 0;  // a new particle set: scenes must be set again
     c->nscenes = 0;
-    c->version++;
     return SPHX_OK;
 }
 
