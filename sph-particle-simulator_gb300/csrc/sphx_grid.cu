@@ -370,17 +370,22 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_partial(
     }
 }
 
+// One warp per sum: lane l adds partials l, l + 32, ... in order, then a fixed shuffle tree
+// (the order never changes, so the sums are reproducible bit for bit).
 __global__ void k_diag_final(const double* __restrict__ part, int nb, DevState* ds) {
-    if (threadIdx.x >= 7) return;
+    const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (k >= 7) return;
     double v = 0;
-    for (int b = 0; b < nb; ++b) v += part[b * kDiagSums + threadIdx.x];
-    ds->sums[threadIdx.x] = v;
+    for (int b = lane; b < nb; b += 32) v += part[b * kDiagSums + k];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) ds->sums[k] = v;
 }
 
 int launch_diag(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds) {
     k_diag_partial<<<b.diag_blocks, kDiagThreads, 0, L.stream>>>(
         b.pos4, b.vel4, b.aux4_s, c.precise ? b.cell4 : nullptr, c.cs_d, c.n, c.grav, b.diag_part);
-    k_diag_final<<<1, 32, 0, L.stream>>>(b.diag_part, b.diag_blocks, ds);
+    k_diag_final<<<1, 7 * 32, 0, L.stream>>>(b.diag_part, b.diag_blocks, ds);
     return 2;
 }
 
