@@ -267,28 +267,25 @@ __device__ __forceinline__ float xdot3(float x, float y, float z) {
 constexpr float kTwoThirds = 0x1.555556p-1f;
 constexpr float kOneSixth = 0x1.555556p-3f;
 
-// CubicSplineKernel::W_3d (kernels.cpp:58-66)
+// CubicSplineKernel::W_3d (kernels.cpp:58-66).  Both branches are evaluated and one is
+// selected: the lanes of a warp hold q on both sides of 1, so a branch would run both
+// paths anyway, plus the divergence handling.
 __device__ __forceinline__ float cubic_w(const StepConst& c, float q) {
-    if (q >= 0.0f && q <= 1.0f) {
-        const float t = xadd(xsub(kTwoThirds, xmul(q, q)), xmul(xmul(xmul(0.5f, q), q), q));
-        return xmul(c.sigma, t);
-    } else if (q > 1.0f && q <= 2.0f) {
-        const float tmp = xsub(2.0f, q);
-        return xmul(c.sigma, xmul(xmul(xmul(kOneSixth, tmp), tmp), tmp));
-    }
-    return 0.0f;
+    const float w1 =
+        xmul(c.sigma, xadd(xsub(kTwoThirds, xmul(q, q)), xmul(xmul(xmul(0.5f, q), q), q)));
+    const float tmp = xsub(2.0f, q);
+    const float w2 = xmul(c.sigma, xmul(xmul(xmul(kOneSixth, tmp), tmp), tmp));
+    return (q >= 0.0f && q <= 1.0f) ? w1 : ((q > 1.0f && q <= 2.0f) ? w2 : 0.0f);
 }
 
 // scalar factor of CubicSplineKernel::gradW_3d (kernels.cpp:96-108):
-// grad = factor * (r / |r|) / h ; r_len >= 1e-6 is the caller's business
+// grad = factor * (r / |r|) / h ; r_len >= 1e-6 is the caller's business.  Branch-free
+// like cubic_w.
 __device__ __forceinline__ float cubic_grad_factor(const StepConst& c, float q) {
-    if (q >= 0.0f && q <= 1.0f) {
-        return xmul(c.sigma, xadd(xmul(-2.0f, q), xmul(xmul(1.5f, q), q)));
-    } else if (q > 1.0f && q <= 2.0f) {
-        const float tmp = xsub(2.0f, q);
-        return xmul(-c.sigma, xmul(xmul(0.5f, tmp), tmp));
-    }
-    return 0.0f;
+    const float f1 = xmul(c.sigma, xadd(xmul(-2.0f, q), xmul(xmul(1.5f, q), q)));
+    const float tmp = xsub(2.0f, q);
+    const float f2 = xmul(-c.sigma, xmul(xmul(0.5f, tmp), tmp));
+    return (q >= 0.0f && q <= 1.0f) ? f1 : ((q > 1.0f && q <= 2.0f) ? f2 : 0.0f);
 }
 
 // CubicSplineKernel::laplacianW_3d (kernels.cpp:130-138).  The branch picks the

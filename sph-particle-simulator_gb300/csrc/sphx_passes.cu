@@ -590,8 +590,8 @@ struct ForceSmem {
     float4 cpos[32], cvel[32], caux[32];
     float4 tpos[32], tvel[32];  // targets: x,y,z,m and vx,vy,vz,P
     uint16_t plist[32 * 32];
-    float4 tbA[kForceBatch];  // pressure term x, y and viscosity term x, y
-    float2 tbB[kForceBatch];  // pressure term z, viscosity term z
+    float4 tbA[kForceBatch];  // -(pressure term) x, y and viscosity term x, y
+    float2 tbB[kForceBatch];  // -(pressure term) z, viscosity term z
 };
 
 // The pair term of particle t against candidate j: the pressure-force contribution
@@ -666,7 +666,10 @@ __device__ __forceinline__ void force_term(const StepConst& c, const float4& xt,
 
 // force_term<CUBIC_SPLINE> with the x and y components of every component-wise step done
 // as packed FP32 pairs (same operations, same rounding, element by element); returns the
-// record (p.x, p.y, v.x, v.y), (p.z, v.z).
+// record (-p.x, -p.y, v.x, v.y), (-p.z, v.z).  The pressure term is stored negated so that
+// the caller's sums are all additions: x - p == x + (-p) in IEEE arithmetic, and the
+// negated products are exact ((-s) * g == -(s * g)).  A skipped term is -0, the negation of
+// the reference's +0 (x + (-0) == x - (+0) == x for every x).
 __device__ __forceinline__ void force_term_cubic_x2(const StepConst& c, const float4& xt,
                                                     const float4& vt, float Pt,
                                                     const float4& xj, const float4& vj,
@@ -676,11 +679,11 @@ __device__ __forceinline__ void force_term_cubic_x2(const StepConst& c, const fl
     const float2 sq = upk2(xmul2(dxy, dxy));
     const float r_len = xsqrt(xadd(xadd(sq.x, sq.y), xmul(dz, dz)));
     const float q = xdiv_fixed(r_len, c.h, c.rcp_h, c.fast_div_h);
-    f32x2 pxy = pk2(0.0f, 0.0f);
-    float pz = 0.0f;
+    f32x2 pxy = pk2(-0.0f, -0.0f);
+    float pz = -0.0f;
     if (!(r_len < 1e-6f)) {
         const float pt = xdiv(xadd(Pt, aj.y), aj.z);
-        const float sp = xmul(xj.w, pt);
+        const float sp = xmul(-xj.w, pt);  // -(m_j * pt)
         f32x2 gxy = pk2(0.0f, 0.0f);
         float gz = 0.0f;
         if ((q >= 0.0f && q <= 1.0f) || (q > 1.0f && q <= 2.0f)) {
@@ -820,8 +823,8 @@ __global__ void __launch_bounds__(128, 7) k_force(const StepConst cp, const Buff
         }
         S->tpos[lane] = xi;
         S->tvel[lane] = make_float4(vi0.x, vi0.y, vi0.z, Pi);
-        f32x2 fpxy = pk2(0.0f, 0.0f), fvxy = pk2(0.0f, 0.0f);  // (x, y) sums, packed
-        float fpz = 0.0f, fvz = 0.0f;
+        // force sums, packed: pressure (x, y), viscosity (x, y), (pressure z, viscosity z)
+        f32x2 fpxy = pk2(0.0f, 0.0f), fvxy = pk2(0.0f, 0.0f), fz = pk2(0.0f, 0.0f);
         KSum Fx, Fy, Fz;  // precision mode: one compensated sum per component
         const uint32_t* rec = slot != kNoSlot ? b.hitmask + (size_t)slot * 32 + lane : nullptr;
         uint32_t mnext =
@@ -901,8 +904,8 @@ __global__ void __launch_bounds__(128, 7) k_force(const StepConst cp, const Buff
                         else
                             force_term<kKern>(c, S->tpos[tt], vt, vt.w, S->cpos[jj],
                                               S->cvel[jj], S->caux[jj], p3, v3);
-                        S->tbA[u] = make_float4(p3[0], p3[1], v3[0], v3[1]);
-                        S->tbB[u] = make_float2(p3[2], v3[2]);
+                        S->tbA[u] = make_float4(-p3[0], -p3[1], v3[0], v3[1]);
+                        S->tbB[u] = make_float2(-p3[2], v3[2]);
                     }
                     __syncwarp();
                     const uint32_t k1 = min(o + cnt, end);
@@ -911,16 +914,15 @@ __global__ void __launch_bounds__(128, 7) k_force(const StepConst cp, const Buff
                         const float4 A = S->tbA[u];
                         const float2 Bv = S->tbB[u];
                         if (kPrecise) {
-                            Fx.add(A.z - A.x);
-                            Fy.add(A.w - A.y);
-                            Fz.add(Bv.y - Bv.x);
+                            Fx.add(A.z + A.x);
+                            Fy.add(A.w + A.y);
+                            Fz.add(Bv.y + Bv.x);
                             continue;
                         }
-                        // a skipped pressure term is +0, and x - (+0) == x exactly
-                        fpxy = xsub2(fpxy, pk2(A.x, A.y));
+                        // the records hold -(pressure term): three packed additions
+                        fpxy = xadd2(fpxy, pk2(A.x, A.y));
                         fvxy = xadd2(fvxy, pk2(A.z, A.w));
-                        fpz = xsub(fpz, Bv.x);
-                        fvz = xadd(fvz, Bv.y);
+                        fz = xadd2(fz, pk2(Bv.x, Bv.y));
                     }
                     __syncwarp();
                 }
@@ -935,7 +937,8 @@ __global__ void __launch_bounds__(128, 7) k_force(const StepConst cp, const Buff
             ay = (Fy.value() + c.grav * mi) / mi;
             az = Fz.value() / mi;
         } else {
-            const float2 fp = upk2(fpxy), fv = upk2(fvxy);
+            const float2 fp = upk2(fpxy), fv = upk2(fvxy), fzz = upk2(fz);
+            const float fpz = fzz.x, fvz = fzz.y;
             ax = xdiv(xadd(xadd(fp.x, fv.x), xmul(0.0f, mi)), mi);
             ay = xdiv(xadd(xadd(fp.y, fv.y), xmul(c.grav, mi)), mi);
             az = xdiv(xadd(xadd(fpz, fvz), xmul(0.0f, mi)), mi);
