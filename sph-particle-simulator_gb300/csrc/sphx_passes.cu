@@ -261,6 +261,13 @@ __device__ __forceinline__ Diff diff(const float4& xi, const float4& xj) {
     d.d2 = xdot3(d.x, d.y, d.z);
     return d;
 }
+// diff(xi, xj).d2 with the x and y steps as packed FP32 pairs (same rounding)
+__device__ __forceinline__ float diff_d2(const float4& xi, const float4& xj) {
+    const f32x2 dxy = xsub2(pk2(xi.x, xi.y), pk2(xj.x, xj.y));
+    const float dz = xsub(xi.z, xj.z);
+    const float2 sq = upk2(xmul2(dxy, dxy));
+    return xadd(xadd(sq.x, sq.y), xmul(dz, dz));
+}
 
 // ---------------------------------------------------------------------------------------
 // Chunk machinery shared by the density and force passes.
@@ -546,8 +553,8 @@ __global__ void __launch_bounds__(128, 10) k_density(const StepConst cp, const B
                             const float dx = xt.x - xj.x, dy = xt.y - xj.y, dz = xt.z - xj.z;
                             S->tbuf[f - base] = xj.w * pair_w_p<kKern>(c, dx * dx + dy * dy + dz * dz);
                         } else {
-                            const Diff d = diff(S->tpos[pr >> 5], xj);
-                            S->tbuf[f - base] = xmul(xj.w, pair_w_exact<kKern>(c, d.d2));
+                            const float d2 = diff_d2(S->tpos[pr >> 5], xj);
+                            S->tbuf[f - base] = xmul(xj.w, pair_w_exact<kKern>(c, d2));
                         }
                     }
                     __syncwarp();
@@ -584,6 +591,14 @@ __global__ void __launch_bounds__(128, 10) k_density(const StepConst cp, const B
 //  sph_engine.cpp:390-443; integrate_leapfrog, cpp:290-310;
 //  ParticleSystem::apply_boundary_conditions, particle.cpp:122-153)
 // ---------------------------------------------------------------------------------------
+// A candidate's (rho, P, 2 rho, m / rho) as the pair terms read it: the last entry
+// multiplied by the viscosity once here, (m_j / rho_j) * mu being the first product of the
+// reference's viscosity term for every target.
+__device__ __forceinline__ float4 stage_aux(float4 a, float visc) {
+    a.w = xmul(a.w, visc);
+    return a;
+}
+
 struct ForceSmem {
     float4 box_lo, box_hi;  // tile box (the fallback walk's culling test)
     int2 seg[kMaxSegments]; // the tile's row segments
@@ -658,7 +673,7 @@ __device__ __forceinline__ void force_term(const StepConst& c, const float4& xt,
         }
         lap = K == SPHX_KERNEL_WENDLAND_C2 ? wendland_lap(c, q) : cubic_lap(c, q);
     }
-    const float sv = xmul(aj.w, c.visc);
+    const float sv = aj.w;  // (m_j / rho_j) * mu, formed when the candidate is staged
     v3[0] = xmul(xmul(sv, xsub(vj.x, vt.x)), lap);
     v3[1] = xmul(xmul(sv, xsub(vj.y, vt.y)), lap);
     v3[2] = xmul(xmul(sv, xsub(vj.z, vt.z)), lap);
@@ -696,7 +711,7 @@ __device__ __forceinline__ void force_term_cubic_x2(const StepConst& c, const fl
         pz = xmul(sp, xdiv_fixed(gz, c.h, c.rcp_h, c.fast_div_h));
     }
     const float lap = cubic_lap(c, q);
-    const float sv = xmul(aj.w, c.visc);
+    const float sv = aj.w;  // (m_j / rho_j) * mu, formed when the candidate is staged
     const f32x2 vxy = xmul2(xmul2(pk2(sv, sv), xsub2(pk2(vj.x, vj.y), pk2(vt.x, vt.y))),
                             pk2(lap, lap));
     const float vz = xmul(xmul(sv, xsub(vj.z, vt.z)), lap);
@@ -742,7 +757,7 @@ __device__ __forceinline__ void force_term_p(const StepConst& c, const float4& x
         p3[1] = s * dy;
         p3[2] = s * dz;
     }
-    const float sv = aj.w * c.visc * lap;
+    const float sv = aj.w * lap;  // aj.w = (m_j / rho_j) * mu
     v3[0] = sv * (vj.x - vt.x);
     v3[1] = sv * (vj.y - vt.y);
     v3[2] = sv * (vj.z - vt.z);
@@ -851,7 +866,7 @@ __global__ void __launch_bounds__(128, 7) k_force(const StepConst cp, const Buff
                         if (kPrecise) pl = frame_pos(b.cell4_s[s + lane], frame, pl, c.cs);
                         S->cpos[lane] = pl;
                         S->cvel[lane] = b.vel4_s[s + lane];
-                        S->caux[lane] = b.aux4_s[s + lane];
+                        S->caux[lane] = stage_aux(b.aux4_s[s + lane], c.visc);
                     }
                     __syncwarp();
                 } else {
@@ -868,7 +883,7 @@ __global__ void __launch_bounds__(128, 7) k_force(const StepConst cp, const Buff
                     if (!surv) continue;
                     if (surv & (1u << lane)) {
                         S->cvel[lane] = b.vel4_s[s + lane];
-                        S->caux[lane] = b.aux4_s[s + lane];
+                        S->caux[lane] = stage_aux(b.aux4_s[s + lane], c.visc);
                     }
                     __syncwarp();
                     mask = valid ? chunk_hits<kPrecise>(S->cpos, surv, xi, c.r2) : 0u;
