@@ -41,6 +41,7 @@ struct sphx_ctx {
     // or the stats are requested, so profiling adds no per-step host sync
     // batched scenes
     uint32_t nscenes = 0;
+    bool scenes_nz = false;  // every scene's divisors admit the untested divisions (div_nz)
     uint32_t scene_cap = 0;
     std::vector<sphx_params> scene_params;
     std::vector<uint64_t> scene_start;
@@ -193,6 +194,12 @@ void fill_step_const_from(sphx_ctx* c, const sphx_params& p, size_t n, StepConst
     s.rcp_hsq = 1.0f / s.h_sq;
     s.fast_div_h = verify_fixed_divisor(h) ? 1 : 0;
     s.fast_div_hsq = verify_fixed_divisor(s.h_sq) ? 1 : 0;
+    // the cubic passes' untested divisions: |r| of a hit is at most r (1 + 2^-23) and the
+    // Laplacian's numerator at most 2 sigma; both divisors verified (so h, h^2 in
+    // [2^-20, 2^20] and sigma = 1/(pi h^3) within [2^-62, 2^59])
+    s.div_nz = s.fast_div_h && s.fast_div_hsq && p.neighbor_search_radius > 0.0f &&
+                       p.neighbor_search_radius <= 0x1p99f
+                   ? 1 : 0;
     s.precise = c->tuning.mode != SPHX_MODE_EXACT;
     s.fp16 = c->tuning.mode == SPHX_MODE_PRECISE_FP16;
     s.cs = p.neighbor_search_radius;
@@ -283,6 +290,7 @@ int run_phases(sphx_ctx* c, float dt, bool integrate) {
         SPHX_CUDA(cudaEventRecord(slot->ev[0], c->stream));
     }
     const bool batch = c->b.nscenes > 0;
+    if (batch) c->sc.div_nz = c->scenes_nz ? 1 : 0;  // the passes' kernels serve all scenes
     int k = 0;
     if (batch) {
         k += launch_batch_begin(c->L, c->b, c->ds);
@@ -873,12 +881,15 @@ int sphx_set_scenes(sphx_ctx* c, uint32_t nscenes, const uint64_t* scene_start,
         fill_step_const_from(c, params[s], si.count, si.c);
         for (uint64_t i = scene_start[s]; i < scene_start[s + 1]; ++i) owner[i] = s;
     }
+    bool all_nz = true;
+    for (const SceneInfo& si : info) all_nz = all_nz && si.c.div_nz;
     SPHX_CUDA(cudaStreamSynchronize(c->stream));
     SPHX_CUDA(cudaMemcpy(b.scenes, info.data(), nscenes * sizeof(SceneInfo), cudaMemcpyHostToDevice));
     if (c->n) SPHX_CUDA(cudaMemcpy(b.scene_of, owner.data(), c->n * sizeof(uint32_t), cudaMemcpyHostToDevice));
     c->scene_params.assign(params, params + nscenes);
     c->scene_start.assign(scene_start, scene_start + nscenes + 1);
     c->nscenes = nscenes;
+    c->scenes_nz = all_nz;
     b.nscenes = (int)nscenes;
     if (!c->have_params) {  // the context-wide parameters default to the first scene's
         c->params = params[0];

@@ -52,6 +52,7 @@ struct StepConst {
     float gg;     // Gaussian -2 sigma_sq_inv_ norm_
     float gl;     // Gaussian 2 sigma_sq_inv_ norm_
     float g2s;    // Gaussian 2 sigma_sq_inv_
+    int div_nz;   // 1: the cubic passes' dividends are in xdiv_fixed_nz's range by bounds
 };
 
 // Device-resident scalars written and read by the kernels of a step.
@@ -207,6 +208,23 @@ __device__ __forceinline__ float xdiv_fixed(float a, float b, float y, int verif
     return __fdiv_rn(a, b);
 }
 
+// xdiv_fixed without the range test, for dividends known to be +-0 or of magnitude in
+// [2^-100, 2^100] with a verified divisor b in [2^-20, 2^20].  In that range q0 and the
+// quotient are normal and the residual r is exact (a multiple of 2^(e_a - 46) >= 2^-146,
+// at most about 2^-22 |a|), so the sequence scales exactly with powers of two of a and
+// the verification on one binade covers every binade.  A zero dividend gives +0 whatever
+// its sign; the callers whose dividend can be -0 restore the sign (xsign).
+__device__ __forceinline__ float xdiv_fixed_nz(float a, float b, float y) {
+    const float q0 = __fmul_rn(a, y);
+    const float r = __fmaf_rn(-q0, b, a);
+    return __fmaf_rn(r, y, q0);
+}
+
+// q with the sign bit of a (q = a / b for b > 0: only a zero quotient can lose it)
+__device__ __forceinline__ float xsign(float q, float a) {
+    return __int_as_float((__float_as_int(q) & 0x7fffffff) | (__float_as_int(a) & (int)0x80000000));
+}
+
 // Packed FP32 pairs (Blackwell f32x2 instructions): two IEEE round-to-nearest operations in
 // one instruction, each element rounded exactly as the scalar __f*_rn would.
 typedef unsigned long long f32x2;
@@ -257,6 +275,15 @@ __device__ __forceinline__ f32x2 xdiv_fixed2(f32x2 a2, float b, float y, int ver
     return pk2(xdiv_fixed(a.x, b, y, verified), xdiv_fixed(a.y, b, y, verified));
 }
 
+// xdiv_fixed_nz of a pair of dividends, signs restored
+__device__ __forceinline__ f32x2 xdiv_fixed2_nz(f32x2 a2, float b, float y) {
+    const f32x2 y2 = pk2(y, y);
+    const f32x2 q0 = xmul2(a2, y2);
+    const f32x2 r = xfma2(q0, pk2(-b, -b), a2);
+    const f32x2 q = xfma2(r, y2, q0);
+    return (q & 0x7fffffff7fffffffull) | (a2 & 0x8000000080000000ull);
+}
+
 // glm::dot(v, v) = (x*x + y*y) + z*z (products rounded first)
 __device__ __forceinline__ float xdot3(float x, float y, float z) {
     return xadd(xadd(xmul(x, x), xmul(y, y)), xmul(z, z));
@@ -292,11 +319,16 @@ __device__ __forceinline__ float cubic_grad_factor(const StepConst& c, float q) 
 // numerator, one division follows: lanes of a warp hold q on both sides of 1, and a
 // division per branch would run twice.  Outside both ranges (and for NaN q) the numerator
 // is 0 and 0 / h_sq = +0, the reference's 0.0f.
+template <bool kNZ = false>
 __device__ __forceinline__ float cubic_lap(const StepConst& c, float q) {
     const float a = (q > 1.0f) ? xsub(2.0f, q) : xadd(-2.0f, xmul(3.0f, q));
     const bool in = (q >= 0.0f && q <= 1.0f) || (q > 1.0f && q <= 2.0f);
     const float num = in ? xmul(c.sigma, a) : 0.0f;
-    return xdiv_fixed(num, c.h_sq, c.rcp_hsq, c.fast_div_hsq);
+    // kNZ: a is 0 or at least 2^-23 in magnitude (2 - q and 3q - 2 are exact multiples of
+    // ulp(q) or of ulp(3q)), so num is +0 or in [sigma 2^-24, 2 sigma], inside
+    // xdiv_fixed_nz's range for the sigma the host admits
+    return kNZ ? xdiv_fixed_nz(num, c.h_sq, c.rcp_hsq)
+               : xdiv_fixed(num, c.h_sq, c.rcp_hsq, c.fast_div_hsq);
 }
 
 // WendlandC2Kernel::W after q = length(r)/h (kernels.cpp:172-178):

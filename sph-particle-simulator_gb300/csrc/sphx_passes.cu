@@ -269,6 +269,10 @@ __device__ __forceinline__ float diff_d2(const float4& xi, const float4& xj) {
     return xadd(xadd(sq.x, sq.y), xmul(dz, dz));
 }
 
+// a gradient component inside xdiv_fixed_nz's range: zero, or at least 2^-100 in
+// magnitude (its upper bound, sigma, is the host's business)
+__device__ __forceinline__ bool nz_range(float g) { return !(fabsf(g) < 0x1p-100f) || g == 0.0f; }
+
 // ---------------------------------------------------------------------------------------
 // Chunk machinery shared by the density and force passes.
 //
@@ -407,10 +411,13 @@ __device__ __forceinline__ float cubic_w_p(const StepConst& c, float q) {
 // W of the pair (x_i - x_j = (dx, dy, dz), d2 = |.|^2) for smoothing kernel K.
 // Exact mode: the reference's float operations (Kernel::W, kernels.cpp:140-143, 172-178,
 // 210-213); precision mode: contracted arithmetic.
-template <int K>
+// kNZ: d2 <= r^2 (a hit), so |r| is +0 or in [2^-74.5, r (1 + 2^-23)], which the host
+// keeps inside xdiv_fixed_nz's range
+template <int K, bool kNZ = false>
 __device__ __forceinline__ float pair_w_exact(const StepConst& c, float d2) {
     if (K == SPHX_KERNEL_GAUSSIAN) return xmul(c.wnorm, expf(xmul(-d2, c.gs)));
-    const float q = xdiv_fixed(xsqrt(d2), c.h, c.rcp_h, c.fast_div_h);
+    const float q = kNZ ? xdiv_fixed_nz(xsqrt(d2), c.h, c.rcp_h)
+                        : xdiv_fixed(xsqrt(d2), c.h, c.rcp_h, c.fast_div_h);
     return K == SPHX_KERNEL_WENDLAND_C2 ? wendland_w(c, q) : cubic_w(c, q);
 }
 template <int K>
@@ -451,7 +458,7 @@ struct DensitySmem {
     float tbuf[kDensityBatch];
 };
 
-template <bool kPrecise, bool kBatch, int kKern>
+template <bool kPrecise, bool kBatch, int kKern, bool kNZ>
 __global__ void __launch_bounds__(128, 10) k_density(const StepConst cp, const Buffers b,
                                                  DevState* ds) {
     if (ds->status) return;
@@ -554,7 +561,7 @@ __global__ void __launch_bounds__(128, 10) k_density(const StepConst cp, const B
                             S->tbuf[f - base] = xj.w * pair_w_p<kKern>(c, dx * dx + dy * dy + dz * dz);
                         } else {
                             const float d2 = diff_d2(S->tpos[pr >> 5], xj);
-                            S->tbuf[f - base] = xmul(xj.w, pair_w_exact<kKern>(c, d2));
+                            S->tbuf[f - base] = xmul(xj.w, pair_w_exact<kKern, kNZ>(c, d2));
                         }
                     }
                     __syncwarp();
@@ -685,6 +692,11 @@ __device__ __forceinline__ void force_term(const StepConst& c, const float4& xt,
 // the caller's sums are all additions: x - p == x + (-p) in IEEE arithmetic, and the
 // negated products are exact ((-s) * g == -(s * g)).  A skipped term is -0, the negation of
 // the reference's +0 (x + (-0) == x - (+0) == x for every x).
+// kNZ: the divisions by h and h^2 without range tests where bounds keep the dividends in
+// xdiv_fixed_nz's range (|r| of a hit, the Laplacian's numerator); the gradient's
+// components are tested once per pair and take the tested divisions only when one of
+// them is nonzero and below 2^-100 in magnitude.
+template <bool kNZ>
 __device__ __forceinline__ void force_term_cubic_x2(const StepConst& c, const float4& xt,
                                                     const float4& vt, float Pt,
                                                     const float4& xj, const float4& vj,
@@ -693,7 +705,8 @@ __device__ __forceinline__ void force_term_cubic_x2(const StepConst& c, const fl
     const float dz = xsub(xt.z, xj.z);
     const float2 sq = upk2(xmul2(dxy, dxy));
     const float r_len = xsqrt(xadd(xadd(sq.x, sq.y), xmul(dz, dz)));
-    const float q = xdiv_fixed(r_len, c.h, c.rcp_h, c.fast_div_h);
+    const float q = kNZ ? xdiv_fixed_nz(r_len, c.h, c.rcp_h)
+                        : xdiv_fixed(r_len, c.h, c.rcp_h, c.fast_div_h);
     f32x2 pxy = pk2(-0.0f, -0.0f);
     float pz = -0.0f;
     if (!(r_len < 1e-6f)) {
@@ -707,10 +720,16 @@ __device__ __forceinline__ void force_term_cubic_x2(const StepConst& c, const fl
             gxy = xmul2(pk2(gf, gf), pk2(xdiv(d.x, r_len), xdiv(d.y, r_len)));
             gz = xmul(gf, xdiv(dz, r_len));
         }
-        pxy = xmul2(pk2(sp, sp), xdiv_fixed2(gxy, c.h, c.rcp_h, c.fast_div_h));
-        pz = xmul(sp, xdiv_fixed(gz, c.h, c.rcp_h, c.fast_div_h));
+        const float2 g = upk2(gxy);
+        if (kNZ && nz_range(g.x) && nz_range(g.y) && nz_range(gz)) {
+            pxy = xmul2(pk2(sp, sp), xdiv_fixed2_nz(gxy, c.h, c.rcp_h));
+            pz = xmul(sp, xsign(xdiv_fixed_nz(gz, c.h, c.rcp_h), gz));
+        } else {
+            pxy = xmul2(pk2(sp, sp), xdiv_fixed2(gxy, c.h, c.rcp_h, c.fast_div_h));
+            pz = xmul(sp, xdiv_fixed(gz, c.h, c.rcp_h, c.fast_div_h));
+        }
     }
-    const float lap = cubic_lap(c, q);
+    const float lap = cubic_lap<kNZ>(c, q);
     const float sv = aj.w;  // (m_j / rho_j) * mu, formed when the candidate is staged
     const f32x2 vxy = xmul2(xmul2(pk2(sv, sv), xsub2(pk2(vj.x, vj.y), pk2(vt.x, vt.y))),
                             pk2(lap, lap));
@@ -803,7 +822,7 @@ __device__ __forceinline__ void integrate_cells(const StepConst& c, float dt, co
     }
 }
 
-template <bool kIntegrate, bool kPrecise, bool kBatch, int kKern>
+template <bool kIntegrate, bool kPrecise, bool kBatch, int kKern, bool kNZ>
 __global__ void __launch_bounds__(128, 7) k_force(const StepConst cp, const Buffers b,
                                                DevState* ds) {
     if (ds->status) return;
@@ -907,7 +926,7 @@ __global__ void __launch_bounds__(128, 7) k_force(const StepConst cp, const Buff
                         if (!kPrecise && kKern == SPHX_KERNEL_CUBIC_SPLINE) {
                             float4 A;
                             float2 Bp;
-                            force_term_cubic_x2(c, S->tpos[tt], vt, vt.w, S->cpos[jj],
+                            force_term_cubic_x2<kNZ>(c, S->tpos[tt], vt, vt.w, S->cpos[jj],
                                                 S->cvel[jj], S->caux[jj], A, Bp);
                             S->tbA[u] = A;
                             S->tbB[u] = Bp;
@@ -1085,22 +1104,26 @@ static int pass_blocks(const LaunchCtx& L) {
     return L.num_sms * bps;
 }
 
-template <bool kPrecise, bool kBatch, int kKern>
+template <bool kPrecise, bool kBatch, int kKern, bool kNZ = false>
 static void launch_density_t(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                              DevState* ds) {
     const int threads = 32 * L.warps_per_block;
     const size_t sm = (size_t)L.warps_per_block * sizeof(DensitySmem);
     static int blocks[5][33] = {};  // by warps per block, requested CTAs per SM (<= 32)
     int& nb = blocks[L.warps_per_block][L.blocks_per_sm < 32 ? L.blocks_per_sm : 32];
-    if (!nb) nb = resident_blocks(L, k_density<kPrecise, kBatch, kKern>, threads, sm);
-    k_density<kPrecise, kBatch, kKern><<<nb, threads, sm, L.stream>>>(c, b, ds);
+    if (!nb) nb = resident_blocks(L, k_density<kPrecise, kBatch, kKern, kNZ>, threads, sm);
+    k_density<kPrecise, kBatch, kKern, kNZ><<<nb, threads, sm, L.stream>>>(c, b, ds);
 }
 
 template <int kKern>
 static void launch_density_k(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                              DevState* ds) {
-    if (b.nscenes > 0) launch_density_t<false, true, kKern>(L, c, b, ds);
-    else if (c.precise) launch_density_t<true, false, kKern>(L, c, b, ds);
+    const bool nz = kKern == SPHX_KERNEL_CUBIC_SPLINE && !c.precise && c.div_nz;
+    if (b.nscenes > 0) {
+        if (nz) launch_density_t<false, true, kKern, true>(L, c, b, ds);
+        else launch_density_t<false, true, kKern>(L, c, b, ds);
+    } else if (c.precise) launch_density_t<true, false, kKern>(L, c, b, ds);
+    else if (nz) launch_density_t<false, false, kKern, true>(L, c, b, ds);
     else launch_density_t<false, false, kKern>(L, c, b, ds);
 }
 
@@ -1111,25 +1134,30 @@ int launch_density(const LaunchCtx& L, const StepConst& c, const Buffers& b, Dev
     return 1;
 }
 
-template <bool kIntegrate, bool kPrecise, bool kBatch, int kKern>
+template <bool kIntegrate, bool kPrecise, bool kBatch, int kKern, bool kNZ = false>
 static void launch_force_t(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                            DevState* ds) {
     const int threads = 32 * L.warps_per_block;
     const size_t sm = (size_t)L.warps_per_block * sizeof(ForceSmem);
     static int blocks[5][33] = {};  // by warps per block, requested CTAs per SM (<= 32)
     int& nb = blocks[L.warps_per_block][L.blocks_per_sm < 32 ? L.blocks_per_sm : 32];
-    if (!nb) nb = resident_blocks(L, k_force<kIntegrate, kPrecise, kBatch, kKern>, threads, sm);
-    k_force<kIntegrate, kPrecise, kBatch, kKern><<<nb, threads, sm, L.stream>>>(c, b, ds);
+    if (!nb)
+        nb = resident_blocks(L, k_force<kIntegrate, kPrecise, kBatch, kKern, kNZ>, threads, sm);
+    k_force<kIntegrate, kPrecise, kBatch, kKern, kNZ><<<nb, threads, sm, L.stream>>>(c, b, ds);
 }
 
 template <int kKern>
 static void launch_force_k(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                            DevState* ds, int integrate) {
+    const bool nz = kKern == SPHX_KERNEL_CUBIC_SPLINE && !c.precise && c.div_nz;
     if (b.nscenes > 0) {
-        if (integrate) launch_force_t<true, false, true, kKern>(L, c, b, ds);
-        else launch_force_t<false, false, true, kKern>(L, c, b, ds);
+        if (integrate) {
+            if (nz) launch_force_t<true, false, true, kKern, true>(L, c, b, ds);
+            else launch_force_t<true, false, true, kKern>(L, c, b, ds);
+        } else launch_force_t<false, false, true, kKern>(L, c, b, ds);
     } else if (integrate) {
         if (c.precise) launch_force_t<true, true, false, kKern>(L, c, b, ds);
+        else if (nz) launch_force_t<true, false, false, kKern, true>(L, c, b, ds);
         else launch_force_t<true, false, false, kKern>(L, c, b, ds);
     } else {
         if (c.precise) launch_force_t<false, true, false, kKern>(L, c, b, ds);
