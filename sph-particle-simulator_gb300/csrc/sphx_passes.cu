@@ -709,7 +709,31 @@ __device__ __forceinline__ void force_term_cubic_x2(const StepConst& c, const fl
                         : xdiv_fixed(r_len, c.h, c.rcp_h, c.fast_div_h);
     f32x2 pxy = pk2(-0.0f, -0.0f);
     float pz = -0.0f;
-    if (!(r_len < 1e-6f)) {
+    if (kNZ) {
+        // branch-free: every value is computed and the skipped cases are selected away (a
+        // pair with |r| < 1e-6 may divide by zero here; its results are discarded)
+        const bool live = !(r_len < 1e-6f);
+        const bool in = (q >= 0.0f && q <= 1.0f) || (q > 1.0f && q <= 2.0f);
+        const float sp = xmul(-xj.w, xdiv(xadd(Pt, aj.y), aj.z));  // -(m_j * pt)
+        const float gf = cubic_grad_factor(c, q);
+        const float2 d = upk2(dxy);
+        const f32x2 gq = xmul2(pk2(gf, gf), pk2(xdiv(d.x, r_len), xdiv(d.y, r_len)));
+        const float gzq = xmul(gf, xdiv(dz, r_len));
+        const f32x2 gxy = in ? gq : pk2(0.0f, 0.0f);
+        const float gz = in ? gzq : 0.0f;
+        const float2 g = upk2(gxy);
+        f32x2 pq;
+        float pzq;
+        if (nz_range(g.x) && nz_range(g.y) && nz_range(gz)) {
+            pq = xmul2(pk2(sp, sp), xdiv_fixed2_nz(gxy, c.h, c.rcp_h));
+            pzq = xmul(sp, xsign(xdiv_fixed_nz(gz, c.h, c.rcp_h), gz));
+        } else {
+            pq = xmul2(pk2(sp, sp), xdiv_fixed2(gxy, c.h, c.rcp_h, c.fast_div_h));
+            pzq = xmul(sp, xdiv_fixed(gz, c.h, c.rcp_h, c.fast_div_h));
+        }
+        pxy = live ? pq : pxy;
+        pz = live ? pzq : pz;
+    } else if (!(r_len < 1e-6f)) {
         const float pt = xdiv(xadd(Pt, aj.y), aj.z);
         const float sp = xmul(-xj.w, pt);  // -(m_j * pt)
         f32x2 gxy = pk2(0.0f, 0.0f);
@@ -720,14 +744,8 @@ __device__ __forceinline__ void force_term_cubic_x2(const StepConst& c, const fl
             gxy = xmul2(pk2(gf, gf), pk2(xdiv(d.x, r_len), xdiv(d.y, r_len)));
             gz = xmul(gf, xdiv(dz, r_len));
         }
-        const float2 g = upk2(gxy);
-        if (kNZ && nz_range(g.x) && nz_range(g.y) && nz_range(gz)) {
-            pxy = xmul2(pk2(sp, sp), xdiv_fixed2_nz(gxy, c.h, c.rcp_h));
-            pz = xmul(sp, xsign(xdiv_fixed_nz(gz, c.h, c.rcp_h), gz));
-        } else {
-            pxy = xmul2(pk2(sp, sp), xdiv_fixed2(gxy, c.h, c.rcp_h, c.fast_div_h));
-            pz = xmul(sp, xdiv_fixed(gz, c.h, c.rcp_h, c.fast_div_h));
-        }
+        pxy = xmul2(pk2(sp, sp), xdiv_fixed2(gxy, c.h, c.rcp_h, c.fast_div_h));
+        pz = xmul(sp, xdiv_fixed(gz, c.h, c.rcp_h, c.fast_div_h));
     }
     const float lap = cubic_lap<kNZ>(c, q);
     const float sv = aj.w;  // (m_j / rho_j) * mu, formed when the candidate is staged
