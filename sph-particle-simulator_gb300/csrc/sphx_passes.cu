@@ -1179,6 +1179,7 @@ static void launch_force_k(const LaunchCtx& L, const StepConst& c, const Buffers
         else launch_force_t<true, false, false, kKern>(L, c, b, ds);
     } else {
         if (c.precise) launch_force_t<false, true, false, kKern>(L, c, b, ds);
+        else if (nz) launch_force_t<false, false, false, kKern, true>(L, c, b, ds);
         else launch_force_t<false, false, false, kKern>(L, c, b, ds);
     }
 }

@@ -184,6 +184,41 @@ def test_gpu_all_particles_in_one_cell_and_coincident(port):
         assert_bits(a, b, k)
 
 
+def test_gpu_tiny_coordinates_near_the_origin(port):
+    """Particles within 1e-36 of the origin (normal and subnormal coordinates) beside
+    particles at the origin, ordinary ones, and ones whose x alone is tiny: pair terms
+    with zero distances and with gradient components below 2^-100, where the passes leave
+    the untested divisions by h for the range-tested ones; fields and one step stay
+    bit-identical to the oracle."""
+    rng = np.random.default_rng(9)
+    tiny = (rng.integers(-6, 7, size=(300, 3)) * 1e-37).astype(np.float32)
+    sub = (rng.integers(-50, 51, size=(100, 3)) * 1e-44).astype(np.float32)
+    zero = np.zeros((20, 3), np.float32)
+    near = (0.01 + rng.random((200, 3)) * 0.02).astype(np.float32)
+    # x tiny or 0 while y, z are ordinary: |r| is ordinary, the x component of r / |r| tiny
+    axis = (0.01 + rng.random((200, 3)) * 0.02).astype(np.float32)
+    axis[:, 0] = (rng.integers(-3, 4, size=200) * 1e-38).astype(np.float32)
+    pos = np.concatenate([tiny, sub, zero, near, axis])
+    assert (np.abs(sub[sub != 0]) < np.finfo(np.float32).tiny).all()
+    vel = (rng.standard_normal(pos.shape) * 0.1).astype(np.float32)
+    mass = np.full(len(pos), 1e-3, np.float32)
+    prm = I.params16(xmin=-1, xmax=1, ymin=-1, ymax=1, zmin=-1, zmax=1)
+    ctx = make_ctx(len(pos), prm, pos, vel, mass)
+    ctx.eval()
+    out = ctx.download()
+    for a, b, k in zip((out["rho"], out["pressure"], out["acc"]),
+                       port.fields(pos, vel, mass, prm), ("rho", "P", "acc")):
+        assert_bits(a, b, k)
+    ctx.step(1e-3)
+    e = O.Engine(port, len(pos))
+    e.initialize(prm)
+    e.add(pos, vel, mass)
+    e.step(1e-3)
+    out, ref = ctx.download(), e.get()
+    for k in ("pos", "vel", "rho", "pressure", "acc"):
+        assert_bits(out[k], ref[k], k)
+
+
 def test_gpu_capacity_and_parameter_errors():
     ctx = sphx.Context(4)
     with pytest.raises(sphx.SphxError) as ei:
