@@ -617,10 +617,10 @@ struct ForceSmem {
 };
 
 // The pair term of particle t against candidate j: the pressure-force contribution
-// m_j * (P_t + P_j)/(2 rho_j) * gradW (subtracted by the caller; +0 when |r| < 1e-6,
-// where the reference skips it: subtracting +0 leaves every float unchanged) and the
-// viscosity contribution ((m_j/rho_j) mu (v_j - v_t)) laplacianW (added), each with the
-// reference's operations.
+// m_j * (P_t + P_j)/(2 rho_j) * gradW (the caller adds its negation, which equals
+// subtracting it; +0 when |r| < 1e-6, where the reference skips it, and adding -0 leaves
+// every float unchanged) and the viscosity contribution ((m_j/rho_j) mu (v_j - v_t))
+// laplacianW (added), each with the reference's operations; aj.w holds (m_j/rho_j) mu.
 template <int K>
 __device__ __forceinline__ void force_term(const StepConst& c, const float4& xt,
                                            const float4& vt, float Pt, const float4& xj,
