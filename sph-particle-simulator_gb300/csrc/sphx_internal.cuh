@@ -123,16 +123,15 @@ struct Buffers {
     uint32_t* scene_s;   // batched mode: scene of each particle (cell-sorted)
     SceneInfo* scenes;   // batched mode: per-scene records
     int nscenes;         // 0: single scene
-    // Hit masks of the density pass, reused by the force pass of the same step: a tile of
-    // cnt particles stores one record of cnt words per chunk of its walk (word = lane: bit
-    // j set if candidate j of the chunk is within r of the lane's particle).  Every warp of
-    // the density grid owns an equal region of the pool and stores its tiles' records one
-    // after another; tile_slot[t] = the tile's first word, or kNoSlot when the tile did
-    // not fit in what was left of the region (the force pass then repeats the distance
-    // tests for that tile).
+    // Hit masks of the density pass, reused by the force pass of the same step: record r
+    // holds 32 words (word = lane: bit j set if candidate j of the chunk is within r of the
+    // lane's particle).  Every warp of the density grid owns an equal region of the pool
+    // and stores its tiles' records one after another, one record per chunk of the tile's
+    // walk; tile_slot[t] = first record, or kNoSlot when the tile did not fit in what was
+    // left of the region (the force pass then repeats the distance tests for that tile).
     uint32_t* hitmask = nullptr;
     uint32_t* tile_slot = nullptr;
-    unsigned long long hitmask_cap = 0;  // words (at most 0xffff0000: offsets are 32-bit)
+    unsigned long long hitmask_cap = 0;  // records
     int radix_blocks;
     int scan_part_cap;
     int diag_blocks;

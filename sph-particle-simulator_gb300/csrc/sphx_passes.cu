@@ -466,8 +466,8 @@ __global__ void __launch_bounds__(128, 10) k_density(const StepConst cp, const B
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     DensitySmem* S = reinterpret_cast<DensitySmem*>(smem_raw_d) + warp;
     const uint32_t ntiles = ds->n_tiles;
-    // this warp's region of the hit-mask pool, filled tile after tile (word offsets fit 32
-    // bits: the pool holds at most 0xffff0000 words)
+    // this warp's region of the hit-mask pool, filled tile after tile (record indices fit
+    // 32 bits: the pool holds at most 0xffff0000 records)
     if (lane == 0) {
         const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
         const uint32_t region = b.hitmask ? (uint32_t)(b.hitmask_cap / nwarps) : 0u;
@@ -502,11 +502,9 @@ __global__ void __launch_bounds__(128, 10) k_density(const StepConst cp, const B
         KSum rk;
         rk.s = rho;
         uint32_t nn = 0;
-        // hit-mask records of this tile: from the warp's cursor on, one per chunk, one word
-        // per particle of the tile
+        // hit-mask records of this tile: from the warp's cursor on, one per chunk
         __syncwarp();
         const uint32_t slot = S->mcur, room = S->mend - slot;
-        const uint32_t stride = (uint32_t)T.cnt;
         uint32_t nrec = 0;
         const int nseg = build_segments(b, g, T, lane, S->seg);
         __syncwarp();
@@ -532,8 +530,8 @@ __global__ void __launch_bounds__(128, 10) k_density(const StepConst cp, const B
                 }
                 const uint32_t surv = __ballot_sync(kFull, box_near(B, pl, r2m));
                 __syncwarp();
-                uint32_t* rec = valid && (nrec + 1) * stride <= room
-                                    ? b.hitmask + slot + nrec * stride + lane : nullptr;
+                uint32_t* rec =
+                    nrec < room ? b.hitmask + (size_t)(slot + nrec) * 32 + lane : nullptr;
                 // streaming stores: the records must not evict the candidate arrays from L2
                 if (!surv) {
                     if (rec) __stcs(rec, 0u);
@@ -577,9 +575,9 @@ __global__ void __launch_bounds__(128, 10) k_density(const StepConst cp, const B
             }
         }
         if (b.hitmask && lane == 0) {
-            const bool fits = nrec * stride <= room;
+            const bool fits = nrec <= room;
             b.tile_slot[t] = fits ? slot : kNoSlot;
-            if (fits) S->mcur = slot + nrec * stride;
+            if (fits) S->mcur = slot + nrec;
         }
         if (valid) {
             if (kPrecise) rho = rk.value();
@@ -880,16 +878,15 @@ __global__ void __launch_bounds__(128, 7) k_force(const StepConst cp, const Buff
         // force sums, packed: pressure (x, y), viscosity (x, y), (pressure z, viscosity z)
         f32x2 fpxy = pk2(0.0f, 0.0f), fvxy = pk2(0.0f, 0.0f), fz = pk2(0.0f, 0.0f);
         KSum Fx, Fy, Fz;  // precision mode: one compensated sum per component
-        // the tile's records: one per chunk, one word per particle of the tile
-        const uint32_t stride = (uint32_t)T.cnt;
-        const uint32_t* rec = slot != kNoSlot ? b.hitmask + slot + lane : nullptr;
-        uint32_t mnext = rec && valid ? __ldcs(rec) : 0u;
+        const uint32_t* rec = slot != kNoSlot ? b.hitmask + (size_t)slot * 32 + lane : nullptr;
+        uint32_t mnext =
+            rec && (size_t)(rec - b.hitmask) < (size_t)b.hitmask_cap * 32 ? __ldcs(rec) : 0u;
         const int nseg = build_segments(b, g, T, lane, S->seg);
         __syncwarp();
         for (int sg = 0; sg < nseg; ++sg) {
             const int2 se = S->seg[sg];
             const int a = se.x, e = se.y;
-            for (int s = a; s < e; s += kTile, rec += rec ? stride : 0) {
+            for (int s = a; s < e; s += kTile, rec += rec ? 32 : 0) {
                 const int m = min(kTile, e - s);
                 uint32_t mask;
                 __syncwarp();
@@ -897,8 +894,8 @@ __global__ void __launch_bounds__(128, 7) k_force(const StepConst cp, const Buff
                     mask = mnext;
                     // the next chunk's record, loaded a chunk ahead (past the tile's last
                     // chunk it reads another tile's record, or nothing at the pool's end)
-                    mnext = valid && (size_t)(rec + stride - b.hitmask) < (size_t)b.hitmask_cap
-                                ? __ldcs(rec + stride) : 0u;
+                    mnext = (size_t)(rec + 32 - b.hitmask) < (size_t)b.hitmask_cap * 32
+                                ? __ldcs(rec + 32) : 0u;
                     const uint32_t used = __reduce_or_sync(kFull, mask);  // candidates hit
                     if (!used) continue;
                     if (used & (1u << lane)) {
