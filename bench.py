@@ -570,9 +570,11 @@ def bench_ours(args, world, rank, local):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "traffic_hit_masks": traffic_masks,
-                     "traffic_note": "DRAM bytes per launch = the particle data (about 1.3x the "
+                     "traffic_note": "DRAM bytes per launch = the particle data (%.1fx the "
                                      "72 B/particle algorithmic bytes) + the hit-mask records "
-                                     "the density pass wrote for this pass (read once)",
+                                     "the density pass wrote for this pass (read once)"
+                                     % ((traffic - traffic_masks) / (72.0 * w.n)
+                                        if traffic and traffic_masks else float("nan")),
                      "kernel": "k_force<true> (force + leapfrog + clamp)",
                      "peak_source": f"{peak_kind} hbm_gbs"},
         "roofline_issue": issue,
