@@ -332,18 +332,61 @@ int64_t orc_query(size_t n, const float* pos, float cell_size, float radius, int
     return total;
 }
 
+/* Lists of particles [i0, i1) into nl[0 .. i1 - i0) (released with free_block). */
+static void query_block(const cell_hash* h, const float* pos, size_t i0, size_t i1, float r2,
+                        i64vec* nl) {
+#pragma omp parallel for schedule(static)
+    for (long long i = (long long)i0; i < (long long)i1; ++i)
+        hash_query(h, pos, pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], r2, &nl[i - (long long)i0]);
+}
+
+static void free_block(i64vec* nl, size_t m) {
+    for (size_t e = 0; e < m; ++e) {
+        free(nl[e].data);
+        nl[e].data = NULL;
+        nl[e].size = nl[e].cap = 0;
+    }
+}
+
+/* particles whose lists are held at a time by the field evaluations */
+enum { kListBlock = 1 << 19 };
+
+int64_t orc_query_subset(size_t n, const float* pos, float cell_size, float radius, size_t nq,
+                         const int64_t* sel, int64_t* counts, int64_t* idx) {
+    cell_hash h;
+    hash_build(&h, n, pos, cell_size);
+    i64vec* nl = (i64vec*)calloc(nq ? nq : 1, sizeof(i64vec));
+    const float r2 = radius * radius;
+#pragma omp parallel for schedule(static)
+    for (long long q = 0; q < (long long)nq; ++q) {
+        const int64_t i = sel[q];
+        hash_query(&h, pos, pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], r2, &nl[q]);
+    }
+    int64_t total = 0;
+    for (size_t q = 0; q < nq; ++q) {
+        counts[q] = (int64_t)nl[q].size;
+        if (idx) memcpy(idx + total, nl[q].data, nl[q].size * sizeof(int64_t));
+        total += (int64_t)nl[q].size;
+        free(nl[q].data);
+    }
+    free(nl);
+    hash_free(&h);
+    return total;
+}
+
 /* ------------------------------------------------------------------------------------ */
 /* field phases                                                                          */
 /* ------------------------------------------------------------------------------------ */
 
 /* compute_densities -> equations::compute_density (src/sph_engine.cpp:203-212, 370-383) */
-static void densities(size_t n, const float* pos, const float* mass, const i64vec* nl,
-                      const kern* k, float* rho) {
+/* Particles [i0, i1); nl[i - i0] is particle i's list. */
+static void densities(size_t i0, size_t i1, const float* pos, const float* mass,
+                      const i64vec* nl, const kern* k, float* rho) {
     const float w0 = w_of(k, 0.0f, 0.0f, 0.0f);
 #pragma omp parallel for schedule(static)
-    for (long long i = 0; i < (long long)n; ++i) {
+    for (long long i = (long long)i0; i < (long long)i1; ++i) {
         float d = mass[i] * w0;
-        const i64vec* L = &nl[i];
+        const i64vec* L = &nl[i - (long long)i0];
         for (size_t e = 0; e < L->size; ++e) {
             const int64_t j = L->data[e];
             if (j == i) continue;
@@ -364,12 +407,12 @@ static void pressures(size_t n, const float* rho, float rest, float gas, float* 
 
 /* compute_forces: pressure force, viscosity force, external force, acceleration
  * (src/sph_engine.cpp:226-244, 390-443) */
-static void forces(size_t n, const float* pos, const float* vel, const float* mass,
-                   const i64vec* nl, const kern* k, const float* rho, const float* P,
-                   float viscosity, float gravity, float* acc) {
+static void forces(size_t i0, size_t i1, const float* pos, const float* vel,
+                   const float* mass, const i64vec* nl, const kern* k, const float* rho,
+                   const float* P, float viscosity, float gravity, float* acc) {
 #pragma omp parallel for schedule(static)
-    for (long long i = 0; i < (long long)n; ++i) {
-        const i64vec* L = &nl[i];
+    for (long long i = (long long)i0; i < (long long)i1; ++i) {
+        const i64vec* L = &nl[i - (long long)i0];
         float fpx = 0.0f, fpy = 0.0f, fpz = 0.0f;
         for (size_t e = 0; e < L->size; ++e) {
             const int64_t j = L->data[e];
@@ -423,13 +466,27 @@ void orc_fields_k(int kind, size_t n, const float* pos, const float* vel, const 
     float prm[16];
     load_params(params16, prm);
     const kern k = make_kernel(kind, prm[3]);
-    i64vec* nl = (i64vec*)calloc(n ? n : 1, sizeof(i64vec));
-    build_lists(n, pos, prm[15], prm[15], nl, NULL);
-    densities(n, pos, mass, nl, &k, rho);
+    /* The lists of a block of particles at a time (the same lists, so the same sums): the
+     * lists of all particles of a 10M state would take about 22 GB. */
+    cell_hash h;
+    hash_build(&h, n, pos, prm[15]);
+    const float r2 = prm[15] * prm[15];
+    i64vec* nl = (i64vec*)calloc(kListBlock, sizeof(i64vec));
+    for (size_t i0 = 0; i0 < n; i0 += kListBlock) {
+        const size_t i1 = n - i0 < kListBlock ? n : i0 + kListBlock;
+        query_block(&h, pos, i0, i1, r2, nl);
+        densities(i0, i1, pos, mass, nl, &k, rho);
+        free_block(nl, i1 - i0);
+    }
     pressures(n, rho, prm[0], prm[1], P);
-    forces(n, pos, vel, mass, nl, &k, rho, P, prm[2], prm[6], acc);
-    for (size_t i = 0; i < n; ++i) free(nl[i].data);
+    for (size_t i0 = 0; i0 < n; i0 += kListBlock) {
+        const size_t i1 = n - i0 < kListBlock ? n : i0 + kListBlock;
+        query_block(&h, pos, i0, i1, r2, nl);
+        forces(i0, i1, pos, vel, mass, nl, &k, rho, P, prm[2], prm[6], acc);
+        free_block(nl, i1 - i0);
+    }
     free(nl);
+    hash_free(&h);
 }
 
 /* ---- FP64 re-evaluation over the same neighbour sets ---------------------------------- */
@@ -488,74 +545,88 @@ void orc_fields_f64_k(int kind, size_t n, const float* pos, const float* vel,
     float prm[16];
     load_params(params16, prm);
     const double h = prm[3], hsq = h * h, sigma = 1.0 / (M_PI * h * h * h);
-    i64vec* nl = (i64vec*)calloc(n ? n : 1, sizeof(i64vec));
-    build_lists(n, pos, prm[15], prm[15], nl, NULL);
+    cell_hash hh;
+    hash_build(&hh, n, pos, prm[15]);
+    const float r2 = prm[15] * prm[15];
+    i64vec* nl = (i64vec*)calloc(kListBlock, sizeof(i64vec));
+    for (size_t i0 = 0; i0 < n; i0 += kListBlock) {
+        const size_t i1 = n - i0 < kListBlock ? n : i0 + kListBlock;
+        query_block(&hh, pos, i0, i1, r2, nl);
 #pragma omp parallel for schedule(static)
-    for (long long i = 0; i < (long long)n; ++i) {
-        double d = (double)mass[i] * w_d(kind, h, sigma, 0.0);
-        for (size_t e = 0; e < nl[i].size; ++e) {
-            const int64_t j = nl[i].data[e];
-            if (j == i) continue;
-            const double rx = (double)pos[3 * i] - (double)pos[3 * j];
-            const double ry = (double)pos[3 * i + 1] - (double)pos[3 * j + 1];
-            const double rz = (double)pos[3 * i + 2] - (double)pos[3 * j + 2];
-            d += (double)mass[j] * w_d(kind, h, sigma, sqrt(rx * rx + ry * ry + rz * rz));
+        for (long long i = (long long)i0; i < (long long)i1; ++i) {
+            const i64vec* L = &nl[i - (long long)i0];
+            double d = (double)mass[i] * w_d(kind, h, sigma, 0.0);
+            for (size_t e = 0; e < L->size; ++e) {
+                const int64_t j = L->data[e];
+                if (j == i) continue;
+                const double rx = (double)pos[3 * i] - (double)pos[3 * j];
+                const double ry = (double)pos[3 * i + 1] - (double)pos[3 * j + 1];
+                const double rz = (double)pos[3 * i + 2] - (double)pos[3 * j + 2];
+                d += (double)mass[j] * w_d(kind, h, sigma, sqrt(rx * rx + ry * ry + rz * rz));
+            }
+            rho[i] = d;
+            P[i] = (double)prm[1] * (d - (double)prm[0]);
         }
-        rho[i] = d;
-        P[i] = (double)prm[1] * (d - (double)prm[0]);
+        free_block(nl, i1 - i0);
     }
+    for (size_t i0 = 0; i0 < n; i0 += kListBlock) {
+        const size_t i1 = n - i0 < kListBlock ? n : i0 + kListBlock;
+        query_block(&hh, pos, i0, i1, r2, nl);
 #pragma omp parallel for schedule(static)
-    for (long long i = 0; i < (long long)n; ++i) {
-        double f[3] = {0, 0, 0}, sa[3] = {0, 0, 0};
-        for (size_t e = 0; e < nl[i].size; ++e) {
-            const int64_t j = nl[i].data[e];
-            if (j == i) continue;
-            const double r[3] = {(double)pos[3 * i] - (double)pos[3 * j],
-                                 (double)pos[3 * i + 1] - (double)pos[3 * j + 1],
-                                 (double)pos[3 * i + 2] - (double)pos[3 * j + 2]};
-            const double rl = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
-            const double q = rl / h;
-            if (rl >= 1e-6) {
-                const double s = (double)mass[j] * (P[i] + P[j]) / (2.0 * rho[j]);
-                if (kind == 0) {
-                    double c = 0.0;
-                    if (q <= 1.0) c = sigma * (-2.0 * q + 1.5 * q * q);
-                    else if (q <= 2.0) c = -sigma * 0.5 * (2.0 - q) * (2.0 - q);
-                    for (int a = 0; a < 3; ++a) {
-                        const double t = s * c * (r[a] / rl) / h;
-                        f[a] -= t;
-                        sa[a] += fabs(t);
-                    }
-                } else {
-                    const double G = g_d(kind, h, rl);
-                    for (int a = 0; a < 3; ++a) {
-                        const double t = s * G * r[a];
-                        f[a] -= t;
-                        sa[a] += fabs(t);
+        for (long long i = (long long)i0; i < (long long)i1; ++i) {
+            const i64vec* L = &nl[i - (long long)i0];
+            double f[3] = {0, 0, 0}, sa[3] = {0, 0, 0};
+            for (size_t e = 0; e < L->size; ++e) {
+                const int64_t j = L->data[e];
+                if (j == i) continue;
+                const double r[3] = {(double)pos[3 * i] - (double)pos[3 * j],
+                                     (double)pos[3 * i + 1] - (double)pos[3 * j + 1],
+                                     (double)pos[3 * i + 2] - (double)pos[3 * j + 2]};
+                const double rl = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+                const double q = rl / h;
+                if (rl >= 1e-6) {
+                    const double s = (double)mass[j] * (P[i] + P[j]) / (2.0 * rho[j]);
+                    if (kind == 0) {
+                        double c = 0.0;
+                        if (q <= 1.0) c = sigma * (-2.0 * q + 1.5 * q * q);
+                        else if (q <= 2.0) c = -sigma * 0.5 * (2.0 - q) * (2.0 - q);
+                        for (int a = 0; a < 3; ++a) {
+                            const double t = s * c * (r[a] / rl) / h;
+                            f[a] -= t;
+                            sa[a] += fabs(t);
+                        }
+                    } else {
+                        const double G = g_d(kind, h, rl);
+                        for (int a = 0; a < 3; ++a) {
+                            const double t = s * G * r[a];
+                            f[a] -= t;
+                            sa[a] += fabs(t);
+                        }
                     }
                 }
+                double lap = 0.0;
+                if (kind != 0) lap = lap_d(kind, h, rl);
+                else if (q <= 1.0) lap = sigma * (-2.0 + 3.0 * q) / hsq;
+                else if (q <= 2.0) lap = sigma * (2.0 - q) / hsq;
+                const double s = (double)mass[j] / rho[j] * (double)prm[2];
+                for (int a = 0; a < 3; ++a) {
+                    const double t = s * ((double)vel[3 * j + a] - (double)vel[3 * i + a]) * lap;
+                    f[a] += t;
+                    sa[a] += fabs(t);
+                }
             }
-            double lap = 0.0;
-            if (kind != 0) lap = lap_d(kind, h, rl);
-            else if (q <= 1.0) lap = sigma * (-2.0 + 3.0 * q) / hsq;
-            else if (q <= 2.0) lap = sigma * (2.0 - q) / hsq;
-            const double s = (double)mass[j] / rho[j] * (double)prm[2];
+            const double m = mass[i];
+            f[1] += (double)prm[6] * m;
+            sa[1] += fabs((double)prm[6] * m);
             for (int a = 0; a < 3; ++a) {
-                const double t = s * ((double)vel[3 * j + a] - (double)vel[3 * i + a]) * lap;
-                f[a] += t;
-                sa[a] += fabs(t);
+                acc[3 * i + a] = f[a] / m;
+                if (sum_abs) sum_abs[3 * i + a] = sa[a] / fabs(m);
             }
         }
-        const double m = mass[i];
-        f[1] += (double)prm[6] * m;
-        sa[1] += fabs((double)prm[6] * m);
-        for (int a = 0; a < 3; ++a) {
-            acc[3 * i + a] = f[a] / m;
-            if (sum_abs) sum_abs[3 * i + a] = sa[a] / fabs(m);
-        }
+        free_block(nl, i1 - i0);
     }
-    for (size_t i = 0; i < n; ++i) free(nl[i].data);
     free(nl);
+    hash_free(&hh);
 }
 
 /* ---- FP64 evaluation on FP64 positions -------------------------------------------------- */
@@ -793,9 +864,9 @@ void orc_engine_step(orc_engine* e, float dt) {
     e->total_q += n;
     if (mx > e->max_nn) e->max_nn = mx;
     const kern k = make_kernel(e->kind, e->prm[3]);
-    densities(n, e->pos, e->mass, e->nl, &k, e->rho);
+    densities(0, n, e->pos, e->mass, e->nl, &k, e->rho);
     pressures(n, e->rho, e->prm[0], e->prm[1], e->P);
-    forces(n, e->pos, e->vel, e->mass, e->nl, &k, e->rho, e->P, e->prm[2], e->prm[6], e->acc);
+    forces(0, n, e->pos, e->vel, e->mass, e->nl, &k, e->rho, e->P, e->prm[2], e->prm[6], e->acc);
     /* integrate_leapfrog (src/sph_engine.cpp:290-310) */
     const float damping = e->prm[7];
 #pragma omp parallel for schedule(static)

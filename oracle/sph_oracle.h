@@ -25,6 +25,12 @@ extern "C" {
 int64_t orc_query(size_t n, const float* pos, float cell_size, float radius, int64_t* counts,
                   int64_t* idx);
 
+/* The lists of the particles sel[0..nq) (insertion indices) among all n particles, as
+ * orc_query gives them, without building the other particles' lists.  Returns the total
+ * number of entries; counts[nq]; idx (optional) gets the concatenated lists. */
+int64_t orc_query_subset(size_t n, const float* pos, float cell_size, float radius, size_t nq,
+                         const int64_t* sel, int64_t* counts, int64_t* idx);
+
 /* One evaluation of density, pressure and acceleration on a given state, in FP32 with the
  * reference's operation order (src/sph_engine.cpp:203-244, 370-443). */
 void orc_fields(size_t n, const float* pos, const float* vel, const float* mass,

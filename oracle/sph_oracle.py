@@ -96,6 +96,9 @@ class Port(_Lib):
     def __init__(self, path: Path = PORT_PATH):
         super().__init__(path)
         L = self.lib
+        L.orc_query_subset.restype = C.c_int64
+        L.orc_query_subset.argtypes = [C.c_size_t, C.c_void_p, C.c_float, C.c_float, C.c_size_t,
+                                       C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_fields_f64.argtypes = [C.c_size_t] + [C.c_void_p] * 8
         L.orc_fields_f64_k.argtypes = [C.c_int, C.c_size_t] + [C.c_void_p] * 8
         L.orc_engine_set_kernel.argtypes = [C.c_void_p, C.c_int]
@@ -111,6 +114,21 @@ class Port(_Lib):
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_render_instances.argtypes = [C.c_void_p, C.c_size_t] + [C.c_void_p] * 4
         L.orc_render_image.argtypes = [C.c_void_p, C.c_size_t] + [C.c_void_p] * 4
+
+    def query_subset(self, pos, radius: float, sel, cell_size: float | None = None):
+        """Neighbour lists (counts, concatenated ids) of the particles `sel` only, in the
+        reference's order, among all particles of `pos`."""
+        pos = _f32(pos).reshape(-1, 3)
+        sel = np.ascontiguousarray(sel, np.int64)
+        cs = radius if cell_size is None else cell_size
+        fn = self.lib.orc_query_subset
+        counts = np.zeros(sel.size, np.int64)
+        total = fn(pos.shape[0], _p(pos), C.c_float(cs), C.c_float(radius), sel.size, _p(sel),
+                   _p(counts), None)
+        idx = np.zeros(max(total, 1), np.int64)
+        fn(pos.shape[0], _p(pos), C.c_float(cs), C.c_float(radius), sel.size, _p(sel),
+           _p(counts), _p(idx))
+        return counts, idx[:total]
 
     def fields_f64(self, pos, vel, mass, params16, want_scale: bool = False, kernel: int = 0):
         pos = _f32(pos).reshape(-1, 3)

@@ -14,9 +14,10 @@
 //    integration phase is fused into the force pass, so integration_time stays 0.
 //    max_neighbors / total_neighbor_queries are exact (the reference's are updated
 //    without synchronisation inside an OpenMP loop, sph_engine.cpp:350-351).
-//  * The kernel classes and create_kernel are provided (kernels.h) for user code; the
-//    equations:: free functions are not: the per-pair equations run only inside step(),
-//    on the GPU.
+//  * The kernel classes, create_kernel (kernels.h) and the equations:: free functions are
+//    provided for user code as host evaluations with the reference's float operations;
+//    step() itself does not call them: its per-pair equations run on the GPU, in the
+//    same order.
 //  * set_kernel_type / get_kernel_type (new) select the smoothing kernel of the step among
 //    the three create_kernel offers.  The reference engine always uses the cubic spline
 //    (sph_engine.cpp:17, 23, 162), which stays the default; the choice survives
@@ -141,6 +142,35 @@ class SPHEngine {
 
 // Integration methods (src/sph_engine.h:144-148); the step always uses leapfrog.
 enum class IntegrationMethod { EULER, VERLET, LEAPFROG };
+
+// The SPH equations of one particle (src/sph_engine.h:150-179), evaluated on the host with
+// the reference's float operations in its order, so that user code calling them gets the
+// reference's numbers.  `neighbors` lists indices into `particles` (self included or not:
+// i itself is skipped).
+namespace equations {
+
+// rho_i = m_i W(0) + sum_{j != i} m_j W(r_ij)
+float compute_density(size_t i, const std::vector<size_t>& neighbors,
+                      const ParticleSystem& particles, const Kernel& kernel);
+// P = k (rho - rho0)
+float compute_pressure(float density, float rest_density, float gas_constant);
+// -sum_{j != i, |r_ij| >= 1e-6} m_j (P_i + P_j) / (2 rho_j) grad W(r_ij)
+glm::vec3 compute_pressure_force(size_t i, const std::vector<size_t>& neighbors,
+                                 const ParticleSystem& particles, const Kernel& kernel,
+                                 const std::vector<float>& pressures,
+                                 const std::vector<float>& densities);
+// sum_{j != i} (m_j / rho_j) mu (v_j - v_i) laplacian W(r_ij)
+glm::vec3 compute_viscosity_force(size_t i, const std::vector<size_t>& neighbors,
+                                  const ParticleSystem& particles, const Kernel& kernel,
+                                  float viscosity, const std::vector<float>& densities);
+// (0, g, 0)
+glm::vec3 compute_external_forces(float gravity);
+// (F_p + F_v + F_ext m) / m
+glm::vec3 compute_acceleration(const glm::vec3& pressure_force,
+                               const glm::vec3& viscosity_force,
+                               const glm::vec3& external_force, float particle_mass);
+
+}  // namespace equations
 
 namespace utils {
 

@@ -306,6 +306,67 @@ void SPHEngine::validate_simulation() const {
                   << ") may affect simulation stability\n";
 }
 
+namespace equations {
+
+float compute_density(size_t i, const std::vector<size_t>& neighbors,
+                      const ParticleSystem& particles, const Kernel& kernel) {
+    const Particle& self = particles[i];
+    float rho = self.mass * kernel.W(glm::vec3(0.0f));
+    for (const size_t j : neighbors) {
+        if (j == i) continue;
+        const Particle& other = particles[j];
+        rho += other.mass * kernel.W(self.position - other.position);
+    }
+    return rho;
+}
+
+float compute_pressure(float density, float rest_density, float gas_constant) {
+    return gas_constant * (density - rest_density);
+}
+
+glm::vec3 compute_pressure_force(size_t i, const std::vector<size_t>& neighbors,
+                                 const ParticleSystem& particles, const Kernel& kernel,
+                                 const std::vector<float>& pressures,
+                                 const std::vector<float>& densities) {
+    const Particle& self = particles[i];
+    glm::vec3 f(0.0f);
+    for (const size_t j : neighbors) {
+        if (j == i) continue;
+        const Particle& other = particles[j];
+        const glm::vec3 r = self.position - other.position;
+        if (glm::length(r) < 1e-6f) continue;  // coincident pair: no direction
+        const float shared = (pressures[i] + pressures[j]) / (2.0f * densities[j]);
+        f -= other.mass * shared * kernel.gradW(r);
+    }
+    return f;
+}
+
+glm::vec3 compute_viscosity_force(size_t i, const std::vector<size_t>& neighbors,
+                                  const ParticleSystem& particles, const Kernel& kernel,
+                                  float viscosity, const std::vector<float>& densities) {
+    const Particle& self = particles[i];
+    glm::vec3 f(0.0f);
+    for (const size_t j : neighbors) {
+        if (j == i) continue;
+        const Particle& other = particles[j];
+        const glm::vec3 r = self.position - other.position;
+        const glm::vec3 dv = other.velocity - self.velocity;
+        const float lap = kernel.laplacianW(r);
+        f += (other.mass / densities[j]) * viscosity * dv * lap;
+    }
+    return f;
+}
+
+glm::vec3 compute_external_forces(float gravity) { return glm::vec3(0.0f, gravity, 0.0f); }
+
+glm::vec3 compute_acceleration(const glm::vec3& pressure_force,
+                               const glm::vec3& viscosity_force,
+                               const glm::vec3& external_force, float particle_mass) {
+    return (pressure_force + viscosity_force + external_force * particle_mass) / particle_mass;
+}
+
+}  // namespace equations
+
 namespace utils {
 
 // create_dam_break_setup (cpp:450-487): a boundary box shell, then a fluid block

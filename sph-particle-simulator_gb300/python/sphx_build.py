@@ -141,15 +141,21 @@ def build_oracle(force: bool = False) -> Path:
 
 
 def build_ref() -> Path | None:
-    """Builds oracle/_ref from the reference sources when they are present."""
-    ref = Path(os.environ.get("SPH_REFERENCE_DIR", "/root/reference"))
-    if not (ref / "src" / "sph_engine.cpp").exists():
-        return None
+    """Builds oracle/_ref from the reference sources when they are present (their location:
+    SPH_REFERENCE_DIR, else the default of oracle/build_ref.sh); None when they are not."""
     so = REPO / "oracle" / "_ref" / "libsph_ref.so"
-    deps = [REPO / "oracle" / "ref_harness.cpp", REPO / "oracle" / "glm_shim" / "glm" / "glm.hpp"]
-    if _stale(so, deps):
-        subprocess.run(["bash", str(REPO / "oracle" / "build_ref.sh"), str(ref)], check=True,
-                       stdout=subprocess.DEVNULL)
+    deps = [REPO / "oracle" / "ref_harness.cpp", REPO / "oracle" / "glm_shim" / "glm" / "glm.hpp",
+            REPO / "oracle" / "build_ref.sh"]
+    if not _stale(so, deps):
+        return so
+    cmd = ["bash", str(REPO / "oracle" / "build_ref.sh")]
+    if os.environ.get("SPH_REFERENCE_DIR"):
+        cmd.append(os.environ["SPH_REFERENCE_DIR"])
+    r = subprocess.run(cmd, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True)
+    if r.returncode == 2:  # no reference checkout on this machine
+        return None
+    if r.returncode != 0:
+        raise RuntimeError("reference build failed:\n" + r.stderr)
     return so
 
 

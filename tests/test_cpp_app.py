@@ -71,3 +71,43 @@ def test_app_run_matches_oracle_engine(built, port, tmp_path, steps, dt):
     assert res["particles"] == rec.shape[0] and res["steps"] == steps
     assert res["hash"] == f"{h:016x}"
     assert np.float32(res["time"]) == np.float32(e.time())
+
+
+@pytest.mark.parametrize("kernel", [0, 1, 2])
+def test_equations_free_functions_match_the_oracle(built, port, tmp_path, kernel):
+    """equations:: through the drop-in headers (host evaluation) on the reference's own
+    neighbour lists: density, pressure and acceleration bit-identical to the oracle's
+    evaluation of the same state (both call the C library's expf for the Gaussian)."""
+    import sph_oracle as O
+    import sphx_inputs as I
+
+    sys.path.insert(0, str(PKG / "python"))
+    import sphx_build
+
+    sphx_build.build_host()
+    exe = tmp_path / "equations_app"
+    src = REPO / "tests" / "cpp" / "equations_app.cpp"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", str(src),
+                    f"-I{PKG / 'host' / 'include'}", f"-I{REPO / 'include'}",
+                    "-idirafter", str(PKG / "host" / "compat"), f"-L{PKG / 'lib'}",
+                    "-lsph_gb300", "-lsphx", f"-Wl,-rpath,{PKG / 'lib'}", "-o", str(exe)],
+                   check=True, capture_output=True, text=True)
+    w = I.scaled_dam_break(3000, seed=13)
+    rng = np.random.default_rng(13)
+    vel = (rng.standard_normal(w.pos.shape) * 0.1).astype(np.float32)
+    counts, idx = port.query(w.pos, float(w.params[15]))
+    inp, outp = tmp_path / "state.bin", tmp_path / "fields.bin"
+    with open(inp, "wb") as f:
+        f.write(np.array([w.n], np.int64).tobytes())
+        f.write(np.array([kernel], np.int32).tobytes())
+        for a in (w.params, w.pos, vel, w.mass):
+            f.write(np.ascontiguousarray(a, np.float32).tobytes())
+        f.write(counts.astype(np.int64).tobytes())
+        f.write(idx.astype(np.int64).tobytes())
+    subprocess.run([str(exe), str(inp), str(outp)], check=True)
+    got = np.fromfile(outp, np.float32)
+    rho, P, acc = port.fields(w.pos, vel, w.mass, w.params, kernel=kernel)
+    n = w.n
+    for a, b, k in ((got[:n], rho, "rho"), (got[n:2 * n], P, "P"),
+                    (got[2 * n:].reshape(n, 3), acc, "acc")):
+        assert O.bits_equal(a, b), O.mismatch_report(a, b, k)
