@@ -274,7 +274,8 @@ int sphx_grid_cell(sphx_grid* grid, int x, int y, int z, int64_t* idx, size_t* c
  * synchronisation a cudaMalloc/cudaFree brings.
  *
  * Computes rho and P (compute_densities / compute_pressures, src/sph_engine.cpp:203-224)
- * of n particles, bit-identical to sphx_eval + sphx_download.  pos_xyz (3n floats), mass
+ * of n particles, bit-identical to sphx_eval + sphx_download on a context with the default
+ * (cubic-spline) kernel in exact mode.  pos_xyz (3n floats), mass
  * (n), rho (n) and pressure (n) are DEVICE pointers owned by the caller, in insertion
  * order; rho or pressure may be NULL.  Enqueued on cuda_stream (NULL: the default
  * stream) and asynchronous: results are ready when that stream reaches the call.
@@ -287,7 +288,12 @@ int sphx_grid_cell(sphx_grid* grid, int x, int y, int z, int64_t* idx, size_t* c
  *  - every call shares the one array: calls that overlap on the GPU (several streams or
  *    host threads at once) race and must be serialised by the caller;
  *  - the first call on a device looks up the array's device address with that device
- *    current; make that first call before any stream capture begins. */
+ *    current; make that first call before any stream capture begins.  The address is
+ *    kept until the process exits: calls after a cudaDeviceReset on that device are not
+ *    supported;
+ *  - the smoothing kernel is always the cubic spline (the reference engine's kernel);
+ *  - the call does not synchronise, so an error a kernel records on the device is not
+ *    returned; rho and pressure are then left as they were. */
 #define SPHX_NOALLOC_MAX_PARTICLES 65536
 #define SPHX_NOALLOC_MAX_CELLS 262144
 int sphx_density_noalloc(const sphx_params* params, size_t n, const float* pos_xyz,

@@ -111,7 +111,6 @@ float host_cubic_w(float sigma, float q) {
     return 0.0f;
 }
 
-void fill_step_const_from(sphx_ctx* c, const sphx_params& p, size_t n, StepConst& s);
 
 // Verifies the one-correction division sequence of xdiv_fixed for divisor b against IEEE
 // float division, for every dividend significand of the binade [1, 2) (about 8 ms).
@@ -144,10 +143,13 @@ bool verify_fixed_divisor(float b) {
     return ok;
 }
 
-void fill_step_const(sphx_ctx* c) { fill_step_const_from(c, c->params, c->n, c->sc); }
+}  // namespace
 
-void fill_step_const_from(sphx_ctx* c, const sphx_params& p, size_t n, StepConst& s) {
-    s.max_cells = c->sc.max_cells;
+namespace sphx {
+
+void step_const_from_params(const sphx_params& p, size_t n, int kernel, int mode,
+                            uint32_t max_cells, StepConst& s) {
+    s.max_cells = max_cells;
     s.n = (int)n;
     // SpatialHash::set_cell_size(neighbor_search_radius): inv = 1.0f / cell
     s.inv_cell = 1.0f / p.neighbor_search_radius;
@@ -160,15 +162,15 @@ void fill_step_const_from(sphx_ctx* c, const sphx_params& p, size_t n, StepConst
     // W(vec3(0)): q = length(0) / h
     const float q0 = std::sqrt(0.0f) / h;
     s.w0 = host_cubic_w(s.sigma, q0);
-    s.kern = c->kernel;
+    s.kern = kernel;
     s.wnorm = s.wl = s.gs = s.gg = s.gl = s.g2s = 0.0f;
-    if (c->kernel == SPHX_KERNEL_WENDLAND_C2) {
+    if (kernel == SPHX_KERNEL_WENDLAND_C2) {
         // WendlandC2Kernel(h) (kernels.cpp:166-170); W(0) as WendlandC2Kernel::W computes it
         s.wnorm = 21.0f / (2.0f * static_cast<float>(M_PI) * h * h * h);
         s.wl = s.wnorm * (5.0f / s.h_sq);
         const float tmp = 1.0f - 0.5f * q0;
         s.w0 = s.wnorm * tmp * tmp * tmp * tmp * (2.0f * q0 + 1.0f);
-    } else if (c->kernel == SPHX_KERNEL_GAUSSIAN) {
+    } else if (kernel == SPHX_KERNEL_GAUSSIAN) {
         // GaussianKernel(h) (kernels.cpp:203-208); W(0) = norm_ * exp(-0 * sigma_sq_inv_)
         s.gs = 1.0f / (h * h);
         s.wnorm = 1.0f / std::pow(static_cast<float>(M_PI) * h * h, 1.5f);
@@ -200,11 +202,21 @@ void fill_step_const_from(sphx_ctx* c, const sphx_params& p, size_t n, StepConst
     s.div_nz = s.fast_div_h && s.fast_div_hsq && p.neighbor_search_radius > 0.0f &&
                        p.neighbor_search_radius <= 0x1p99f
                    ? 1 : 0;
-    s.precise = c->tuning.mode != SPHX_MODE_EXACT;
-    s.fp16 = c->tuning.mode == SPHX_MODE_PRECISE_FP16;
+    s.precise = mode != SPHX_MODE_EXACT;
+    s.fp16 = mode == SPHX_MODE_PRECISE_FP16;
     s.cs = p.neighbor_search_radius;
     s.cs_d = (double)p.neighbor_search_radius;
 }
+
+}  // namespace sphx
+
+namespace {
+
+void fill_step_const_from(sphx_ctx* c, const sphx_params& p, size_t n, StepConst& s) {
+    step_const_from_params(p, n, c->kernel, c->tuning.mode, c->sc.max_cells, s);
+}
+
+void fill_step_const(sphx_ctx* c) { fill_step_const_from(c, c->params, c->n, c->sc); }
 
 __global__ void k_mass_of(int n, const float4* __restrict__ pos4, float* __restrict__ mass) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -592,6 +604,7 @@ int sphx_create(sphx_ctx** out, size_t capacity, const sphx_tuning* tuning) {
     c->stream = c->own_stream;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    c->L.device = c->device;
     c->L.num_sms = sms > 0 ? sms : 1;
     c->L.warps_per_block = c->tuning.warps_per_block;
     c->L.blocks_per_sm = c->tuning.blocks_per_sm;

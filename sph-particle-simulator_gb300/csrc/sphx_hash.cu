@@ -139,6 +139,7 @@ int sphx_grid_create(sphx_grid** out, size_t capacity) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g->device);
     g->L.stream = g->stream;
+    g->L.device = g->device;
     g->L.num_sms = sms > 0 ? sms : 1;
     g->L.warps_per_block = 4;
     g->capacity = capacity;

@@ -376,9 +376,17 @@ struct KSum {
 
 __device__ __forceinline__ float round_half(float x) { return __half2float(__float2half_rn(x)); }
 
+// ---- host-side constants -------------------------------------------------------------
+// The StepConst of one parameter block, for `n` particles, smoothing kernel `kernel`
+// (SPHX_KERNEL_*) and mode `mode` (SPHX_MODE_*): every constant computed with the
+// reference's float operations, the fixed-divisor checks run (cached per divisor).
+void step_const_from_params(const sphx_params& p, size_t n, int kernel, int mode,
+                            uint32_t max_cells, StepConst& s);
+
 // ---- launch wrappers (host) --------------------------------------------------------
 struct LaunchCtx {
     cudaStream_t stream;
+    int device;  // CUDA device the launches go to (keys per-device launch-shape caches)
     int num_sms;
     int warps_per_block;
     int blocks_per_sm;

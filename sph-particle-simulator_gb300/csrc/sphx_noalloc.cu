@@ -24,7 +24,12 @@
 //    two host threads) race on the array and must be serialised by the caller;
 //  - the first call on a device looks up the array's device address
 //    (cudaGetSymbolAddress) with that device current; make that first call before any
-//    stream capture begins.
+//    stream capture begins.  The address is kept for the life of the process: calls
+//    after a cudaDeviceReset (or any other teardown of the device's primary context) are
+//    not supported;
+//  - the call does not synchronise, so an error a kernel records on the device is not
+//    returned; when one occurs rho and pressure are left as they were;
+//  - the smoothing kernel is always the cubic spline (the reference engine's).
 #include <cmath>
 #include <mutex>
 
@@ -94,15 +99,20 @@ int setup_device(int dev, unsigned char** addr, int* sms) {
     return SPHX_OK;
 }
 
-// W_3d (kernels.cpp:58-66) on the host, for the self term W(0); built with
-// -ffp-contract=off like the rest of the library's host code.
-float noalloc_cubic_w(float sigma, float q) {
-    if (q >= 0.0f && q <= 1.0f) return sigma * (2.0f / 3.0f - q * q + 0.5f * q * q * q);
-    if (q > 1.0f && q <= 2.0f) {
-        const float tmp = 2.0f - q;
-        return sigma * (1.0f / 6.0f * tmp * tmp * tmp);
+// rho and P of the sorted particles back to the caller's arrays in insertion order --
+// skipped entirely when a kernel of this call recorded a device-side error, so that the
+// caller's buffers keep what they held instead of a partial result.
+__global__ void k_noalloc_unpack(int n, const DevState* __restrict__ ds,
+                                 const uint32_t* __restrict__ id_s,
+                                 const float4* __restrict__ aux4_s, float* __restrict__ rho,
+                                 float* __restrict__ pressure) {
+    if (ds->status) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t id = id_s[i];
+        const float4 a = aux4_s[i];
+        if (rho) rho[id] = a.x;
+        if (pressure) pressure[id] = a.y;
     }
-    return 0.0f;
 }
 
 }  // namespace
@@ -123,30 +133,10 @@ extern "C" int sphx_density_noalloc(const sphx_params* p, size_t n, const float*
     int rc = setup_device(dev, &base, &sms);
     if (rc) return rc;
 
-    // the step constants, computed exactly as sphx_set_params / sphx_eval do
+    // the step constants of sphx_set_params + sphx_eval on a context with the default
+    // (cubic-spline) kernel in exact mode: this entry point always uses the cubic spline
     StepConst c{};
-    c.n = (int)n;
-    c.inv_cell = 1.0f / r;
-    c.r2 = r * r;
-    const float h = p->smoothing_length;
-    c.h = h;
-    c.h_sq = h * h;
-    c.sigma = 1.0f / (static_cast<float>(M_PI) * h * h * h);
-    c.w0 = noalloc_cubic_w(c.sigma, std::sqrt(0.0f) / h);
-    c.rest = p->rest_density;
-    c.gas = p->gas_constant;
-    c.visc = p->viscosity;
-    c.grav = p->gravity;
-    c.damping = p->damping;
-    c.cfl = p->cfl_factor;
-    c.timestep = p->timestep;
-    c.lo[0] = p->xmin;
-    c.hi[0] = p->xmax;
-    c.lo[1] = p->ymin;
-    c.hi[1] = p->ymax;
-    c.lo[2] = p->zmin;
-    c.hi[2] = p->zmax;
-    c.max_cells = (uint32_t)kCells;
+    step_const_from_params(*p, n, SPHX_KERNEL_CUBIC_SPLINE, SPHX_MODE_EXACT, (uint32_t)kCells, c);
 
     Buffers b{};
     b.pos4 = reinterpret_cast<float4*>(base + kOffPos4);
@@ -173,6 +163,7 @@ extern "C" int sphx_density_noalloc(const sphx_params* p, size_t n, const float*
 
     LaunchCtx L{};
     L.stream = static_cast<cudaStream_t>(cuda_stream);
+    L.device = dev;
     L.num_sms = sms;
     L.warps_per_block = 4;
     L.blocks_per_sm = 0;
@@ -183,7 +174,8 @@ extern "C" int sphx_density_noalloc(const sphx_params* p, size_t n, const float*
     launch_begin_step(L, ds, 1);
     launch_build_grid(L, c, b, ds);
     launch_density(L, c, b, ds);
-    launch_unpack_sorted(L, (int)n, b.id_s, b.aux4_s, nullptr, rho, pressure, nullptr);
+    const int ub = (int)((n + 255) / 256) < 4 * sms ? (int)((n + 255) / 256) : 4 * sms;
+    k_noalloc_unpack<<<ub, 256, 0, L.stream>>>((int)n, ds, b.id_s, b.aux4_s, rho, pressure);
     if (cudaGetLastError() != cudaSuccess) return SPHX_ERR_CUDA;
     return SPHX_OK;
 }

@@ -18,6 +18,8 @@
 // some lane is that close to a face (guard band eps below).  Every distance test and
 // every term uses the reference's float operations in the reference's order with
 // IEEE round-to-nearest and no contraction, so each lane's sums are bit-identical.
+#include <atomic>
+
 #include "sphx_internal.cuh"
 
 namespace sphx {
@@ -1117,6 +1119,32 @@ static int resident_blocks(const LaunchCtx& L, K kernel, int threads, size_t sme
     return L.num_sms * per_sm;
 }
 
+// Grid sizes of the persistent passes, found once per (device, kernel instantiation, warps
+// per block, requested CTAs per SM) and kept: one cache object per instantiation, indexed
+// by device; any host thread may fill an entry (a racing fill stores the same value).
+constexpr int kMaxCacheDevices = 64;
+struct LaunchShapeCache {
+    std::atomic<int> nb[kMaxCacheDevices][5][33];
+    std::atomic<int>& at(const LaunchCtx& L) {
+        const int d = L.device >= 0 && L.device < kMaxCacheDevices ? L.device : 0;
+        const int w = L.warps_per_block >= 0 && L.warps_per_block <= 4 ? L.warps_per_block : 4;
+        const int b = L.blocks_per_sm >= 0 && L.blocks_per_sm < 32 ? L.blocks_per_sm : 32;
+        return nb[d][w][b];
+    }
+};
+
+template <class K>
+static int cached_resident_blocks(LaunchShapeCache& cache, const LaunchCtx& L, K kernel,
+                                  int threads, size_t smem) {
+    std::atomic<int>& slot = cache.at(L);
+    int nb = slot.load(std::memory_order_relaxed);
+    if (!nb) {
+        nb = resident_blocks(L, kernel, threads, smem);
+        slot.store(nb, std::memory_order_relaxed);
+    }
+    return nb;
+}
+
 static int pass_blocks(const LaunchCtx& L) {
     const int bps = L.blocks_per_sm > 0 ? L.blocks_per_sm : 8;
     return L.num_sms * bps;
@@ -1127,9 +1155,9 @@ static void launch_density_t(const LaunchCtx& L, const StepConst& c, const Buffe
                              DevState* ds) {
     const int threads = 32 * L.warps_per_block;
     const size_t sm = (size_t)L.warps_per_block * sizeof(DensitySmem);
-    static int blocks[5][33] = {};  // by warps per block, requested CTAs per SM (<= 32)
-    int& nb = blocks[L.warps_per_block][L.blocks_per_sm < 32 ? L.blocks_per_sm : 32];
-    if (!nb) nb = resident_blocks(L, k_density<kPrecise, kBatch, kKern, kNZ>, threads, sm);
+    static LaunchShapeCache cache;
+    const int nb = cached_resident_blocks(cache, L, k_density<kPrecise, kBatch, kKern, kNZ>,
+                                          threads, sm);
     k_density<kPrecise, kBatch, kKern, kNZ><<<nb, threads, sm, L.stream>>>(c, b, ds);
 }
 
@@ -1157,10 +1185,9 @@ static void launch_force_t(const LaunchCtx& L, const StepConst& c, const Buffers
                            DevState* ds) {
     const int threads = 32 * L.warps_per_block;
     const size_t sm = (size_t)L.warps_per_block * sizeof(ForceSmem);
-    static int blocks[5][33] = {};  // by warps per block, requested CTAs per SM (<= 32)
-    int& nb = blocks[L.warps_per_block][L.blocks_per_sm < 32 ? L.blocks_per_sm : 32];
-    if (!nb)
-        nb = resident_blocks(L, k_force<kIntegrate, kPrecise, kBatch, kKern, kNZ>, threads, sm);
+    static LaunchShapeCache cache;
+    const int nb = cached_resident_blocks(
+        cache, L, k_force<kIntegrate, kPrecise, kBatch, kKern, kNZ>, threads, sm);
     k_force<kIntegrate, kPrecise, kBatch, kKern, kNZ><<<nb, threads, sm, L.stream>>>(c, b, ds);
 }
 

@@ -76,3 +76,28 @@ def test_noalloc_rejects_sizes_beyond_its_maximum():
     with pytest.raises(sphx.SphxError) as ei:
         sphx.density_noalloc(I.params16(), n, pos.data_ptr(), mass.data_ptr(), rho.data_ptr(), None)
     assert ei.value.code == -5
+
+
+def test_noalloc_second_call_takes_no_device_memory():
+    """After a first call on the device (which looks up the array's address and loads
+    the kernels), further calls leave the device's free memory exactly as it was: the
+    working memory is the library's fixed array, nothing is allocated per call."""
+    torch = pytest.importorskip("torch")
+    w = cluster_workload()
+    dev = torch.device("cuda", 0)
+    pos = torch.from_numpy(np.ascontiguousarray(w.pos)).to(dev)
+    mass = torch.from_numpy(np.ascontiguousarray(w.mass)).to(dev)
+    rho = torch.empty((w.n,), dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def call():
+        sphx.density_noalloc(w.params, w.n, pos.data_ptr(), mass.data_ptr(), rho.data_ptr(),
+                             None, stream.cuda_stream)
+        torch.cuda.synchronize(dev)
+
+    call()
+    free0, _ = torch.cuda.mem_get_info(dev)
+    for _ in range(3):
+        call()
+    free1, _ = torch.cuda.mem_get_info(dev)
+    assert free1 == free0, (free0, free1)
