@@ -245,6 +245,15 @@ int sphx_restore(sphx_ctx* ctx);
  * (sphx_download returns zeros for them until the next step or eval). */
 int sphx_debug_pairs(sphx_ctx* ctx, int64_t* counts, int64_t* idx, size_t* total_inout);
 
+/* sphx_debug_pairs for the particles sel[0 .. nsel) (insertion indices, in [0, n)) only:
+ * counts[q] = |N(sel[q])| and, when idx != NULL and *total_inout is large enough, their
+ * lists concatenated in sel's order, each in the reference's order (the lists
+ * SpatialHash::query_squared gives update_neighbor_lists, src/sph_engine.cpp:335-353).  The
+ * same walk as sphx_debug_pairs; for checking samples of states too large for every list
+ * at once.  Test hook; synchronises; rebuilds the cell grid like sphx_debug_pairs. */
+int sphx_debug_pairs_subset(sphx_ctx* ctx, size_t nsel, const int64_t* sel, int64_t* counts,
+                            int64_t* idx, size_t* total_inout);
+
 /* ---- standalone spatial hash (SpatialHash, src/spatial_hash.h:12-88) --------------------
  * A cell grid of arbitrary positions on the GPU with the reference's query semantics:
  * sphx_grid_query returns, for every query point p, the indices j with

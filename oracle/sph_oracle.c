@@ -659,6 +659,12 @@ static size_t cell_lower(const cell_item* it, size_t n, int64_t x, int64_t y, in
 
 int64_t orc_fields_f64d(size_t n, const double* pos, const float* vel, const float* mass,
                         const float* params16, double* rho, double* P, double* acc) {
+    return orc_fields_f64d_s(n, pos, vel, mass, params16, rho, P, acc, NULL);
+}
+
+int64_t orc_fields_f64d_s(size_t n, const double* pos, const float* vel, const float* mass,
+                          const float* params16, double* rho, double* P, double* acc,
+                          double* sum_abs) {
     float prm[16];
     load_params(params16, prm);
     const double h = prm[3], hsq = h * h, sigma = 1.0 / (M_PI * h * h * h);
@@ -714,7 +720,7 @@ int64_t orc_fields_f64d(size_t n, const double* pos, const float* vel, const flo
     }
 #pragma omp parallel for schedule(dynamic, 256)
     for (long long i = 0; i < (long long)n; ++i) {
-        double f[3] = {0, 0, 0};
+        double f[3] = {0, 0, 0}, sa[3] = {0, 0, 0};
         if (ok[i]) {
             const double* pi = pos + 3 * i;
             for (int dx = -2; dx <= 2; ++dx)
@@ -736,20 +742,32 @@ int64_t orc_fields_f64d(size_t n, const double* pos, const float* vel, const flo
                                 if (q <= 1.0) c = sigma * (-2.0 * q + 1.5 * q * q);
                                 else if (q <= 2.0) c = -sigma * 0.5 * (2.0 - q) * (2.0 - q);
                                 const double s = (double)mass[j] * (P[i] + P[j]) / (2.0 * rho[j]);
-                                for (int a = 0; a < 3; ++a) f[a] -= s * c * (rv[a] / rl) / h;
+                                for (int a = 0; a < 3; ++a) {
+                                    const double t = s * c * (rv[a] / rl) / h;
+                                    f[a] -= t;
+                                    sa[a] += fabs(t);
+                                }
                             }
                             double lap = 0.0;
                             if (q <= 1.0) lap = sigma * (-2.0 + 3.0 * q) / hsq;
                             else if (q <= 2.0) lap = sigma * (2.0 - q) / hsq;
                             const double s = (double)mass[j] / rho[j] * (double)prm[2];
-                            for (int a = 0; a < 3; ++a)
-                                f[a] += s * ((double)vel[3 * j + a] - (double)vel[3 * i + a]) * lap;
+                            for (int a = 0; a < 3; ++a) {
+                                const double t =
+                                    s * ((double)vel[3 * j + a] - (double)vel[3 * i + a]) * lap;
+                                f[a] += t;
+                                sa[a] += fabs(t);
+                            }
                         }
                     }
         }
         const double mm = mass[i];
         f[1] += (double)prm[6] * mm;
-        for (int a = 0; a < 3; ++a) acc[3 * i + a] = f[a] / mm;
+        sa[1] += fabs((double)prm[6] * mm);
+        for (int a = 0; a < 3; ++a) {
+            acc[3 * i + a] = f[a] / mm;
+            if (sum_abs) sum_abs[3 * i + a] = sa[a] / fabs(mm);
+        }
     }
     free(it);
     free(cell_of);

@@ -59,6 +59,11 @@ void orc_fields_f64_k(int kind, size_t n, const float* pos, const float* vel,
  * with the reference's formulas.  Returns the total number of (i, j) pairs. */
 int64_t orc_fields_f64d(size_t n, const double* pos, const float* vel, const float* mass,
                         const float* params16, double* rho, double* P, double* acc);
+/* orc_fields_f64d plus, when sum_abs != NULL, the per-component sum of |term| / m of each
+ * acceleration (the conditioning scale of orc_fields_f64). */
+int64_t orc_fields_f64d_s(size_t n, const double* pos, const float* vel, const float* mass,
+                          const float* params16, double* rho, double* P, double* acc,
+                          double* sum_abs);
 
 /* ---- engine: restatement of SPHEngine state and step (src/sph_engine.cpp:13-353) ---- */
 typedef struct orc_engine orc_engine;

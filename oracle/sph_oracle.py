@@ -104,6 +104,8 @@ class Port(_Lib):
         L.orc_engine_set_kernel.argtypes = [C.c_void_p, C.c_int]
         L.orc_fields_f64d.argtypes = [C.c_size_t] + [C.c_void_p] * 7
         L.orc_fields_f64d.restype = C.c_int64
+        L.orc_fields_f64d_s.argtypes = [C.c_size_t] + [C.c_void_p] * 8
+        L.orc_fields_f64d_s.restype = C.c_int64
         L.orc_engine_get.argtypes = [C.c_void_p] + [C.c_void_p] * 5
         L.orc_engine_set_state.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_engine_last_dt.restype = C.c_float
@@ -144,8 +146,9 @@ class Port(_Lib):
                                   _p(P), _p(acc), _p(scale))
         return (rho, P, acc, scale) if want_scale else (rho, P, acc)
 
-    def fields_f64d(self, pos64, vel, mass, params16):
-        """FP64 density, pressure, acceleration on FP64 positions (sets in FP64)."""
+    def fields_f64d(self, pos64, vel, mass, params16, want_scale: bool = False):
+        """FP64 density, pressure, acceleration on FP64 positions (sets in FP64); with
+        want_scale also the per-component sum of |term| / m of each acceleration."""
         pos64 = np.ascontiguousarray(pos64, np.float64).reshape(-1, 3)
         n = pos64.shape[0]
         vel = _f32(vel).reshape(n, 3)
@@ -154,9 +157,10 @@ class Port(_Lib):
         rho = np.zeros(n)
         P = np.zeros(n)
         acc = np.zeros((n, 3))
-        pairs = self.lib.orc_fields_f64d(n, _p(pos64), _p(vel), _p(mass), _p(prm), _p(rho),
-                                         _p(P), _p(acc))
-        return rho, P, acc, pairs
+        scale = np.zeros((n, 3)) if want_scale else None
+        pairs = self.lib.orc_fields_f64d_s(n, _p(pos64), _p(vel), _p(mass), _p(prm), _p(rho),
+                                           _p(P), _p(acc), _p(scale))
+        return (rho, P, acc, pairs, scale) if want_scale else (rho, P, acc, pairs)
 
     def render_instances(self, rp, pos, vel, colors=None):
         """(n, 20) float32: clip-space corners and colour of every particle.  rp is a

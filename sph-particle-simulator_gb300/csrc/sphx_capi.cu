@@ -1272,6 +1272,77 @@ int sphx_debug_pairs(sphx_ctx* c, int64_t* counts, int64_t* idx, size_t* total_i
     return SPHX_OK;
 }
 
+int sphx_debug_pairs_subset(sphx_ctx* c, size_t nsel, const int64_t* sel, int64_t* counts,
+                            int64_t* idx, size_t* total_inout) {
+    int rc = enter(c);
+    if (rc) return rc;
+    if ((nsel && (!sel || !counts)) || !total_inout) return SPHX_ERR_INVALID_ARG;
+    if (!c->have_params) return SPHX_ERR_NOT_READY;
+    const size_t n = c->n;
+    for (size_t q = 0; q < nsel; ++q)
+        if (sel[q] < 0 || (size_t)sel[q] >= n) return SPHX_ERR_INVALID_ARG;
+    if (nsel == 0) {
+        *total_inout = 0;
+        return SPHX_OK;
+    }
+    fill_step_const(c);
+    c->have_fields = false;  // the grid rebuild below replaces the sorted permutation
+    launch_begin_step(c->L, c->ds, 1);
+    launch_build_grid(c->L, c->sc, c->b, c->ds);
+    uint32_t* d_cnt = nullptr;
+    if ((rc = dmalloc(&d_cnt, n))) return rc;
+    launch_pair_counts(c->L, c->sc, c->b, c->ds, d_cnt);
+    std::vector<uint32_t> h_cnt(n);
+    cudaError_t e = cudaMemcpyAsync(h_cnt.data(), d_cnt, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d_cnt);
+    if (e != cudaSuccess) return cuda_fail(e);
+    rc = sync_status(c);
+    if (rc) return rc;
+    // each distinct selected particle's list once, at off[id]; kNoPairs for the others
+    std::vector<uint64_t> off(n, kNoPairs);
+    uint64_t uniq_total = 0, total = 0;
+    for (size_t q = 0; q < nsel; ++q) {
+        const size_t id = (size_t)sel[q];
+        counts[q] = h_cnt[id];
+        total += h_cnt[id];
+        if (off[id] == kNoPairs) {
+            off[id] = uniq_total;
+            uniq_total += h_cnt[id];
+        }
+    }
+    const size_t cap = *total_inout;
+    *total_inout = (size_t)total;
+    if (!idx) return SPHX_OK;
+    if (cap < total) return SPHX_ERR_OVERFLOW;
+    uint64_t* d_off = nullptr;
+    int64_t* d_out = nullptr;
+    if ((rc = dmalloc(&d_off, n))) return rc;
+    if ((rc = dmalloc(&d_out, uniq_total))) {
+        cudaFree(d_off);
+        return rc;
+    }
+    std::vector<int64_t> lists(uniq_total ? uniq_total : 1);
+    e = cudaMemcpyAsync(d_off, off.data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) {
+        launch_pair_fill(c->L, c->sc, c->b, c->ds, d_off, d_out);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && uniq_total)
+        e = cudaMemcpyAsync(lists.data(), d_out, uniq_total * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d_off);
+    cudaFree(d_out);
+    if (e != cudaSuccess) return cuda_fail(e);
+    uint64_t at = 0;
+    for (size_t q = 0; q < nsel; ++q) {
+        const size_t id = (size_t)sel[q];
+        std::memcpy(idx + at, lists.data() + off[id], h_cnt[id] * sizeof(int64_t));
+        at += h_cnt[id];
+    }
+    return SPHX_OK;
+}
+
 void sphx_camera_matrices(const float position[3], float yaw_deg, float pitch_deg,
                           float fov_deg, float aspect, float view[16], float projection[16]) {
     const float rad = 0.01745329251994329577f;

@@ -137,6 +137,7 @@ struct Buffers {
     int diag_blocks;
 };
 constexpr uint32_t kNoSlot = 0xffffffffu;
+constexpr uint64_t kNoPairs = ~0ull;  // pair fill: this particle's list is not wanted
 
 // Device generation of initial conditions (sphx_gen.cu): one shape, its constants derived
 // on the host with the generator's float operations.

@@ -1076,6 +1076,7 @@ __global__ void __launch_bounds__(128) k_pairs(const StepConst c, const Buffers 
         const int i = T.k0 + lane;
         const uint32_t id = valid ? b.id_s[i] : 0u;
         uint64_t pos = (kFill && valid) ? off_by_id[id] : 0ull;
+        const bool want = !kFill || pos != kNoPairs;  // fill: particles with an offset only
         uint32_t nn = 0;
         for_each_row(b, g, T, [&](int a, int e) {
             for (int s = a; s < e; s += kTile) {
@@ -1097,7 +1098,7 @@ __global__ void __launch_bounds__(128) k_pairs(const StepConst c, const Buffers 
                         d2 = diff(xi, cand[jj]).d2;
                     }
                     if (valid && d2 <= c.r2) {
-                        if (kFill) out[pos++] = (int64_t)b.id_s[s + jj];
+                        if (kFill && want) out[pos++] = (int64_t)b.id_s[s + jj];
                         ++nn;
                     }
                 }

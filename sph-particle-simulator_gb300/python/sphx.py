@@ -41,7 +41,8 @@ EXPORTS = (
     "sphx_set_params", "sphx_upload", "sphx_upload_f64", "sphx_step", "sphx_eval",
     "sphx_download", "sphx_download_f64", "sphx_get_time_f64",
     "sphx_size", "sphx_get_time", "sphx_set_time", "sphx_get_stats", "sphx_reset_stats",
-    "sphx_snapshot", "sphx_restore", "sphx_debug_pairs", "sphx_grid_create",
+    "sphx_snapshot", "sphx_restore", "sphx_debug_pairs", "sphx_debug_pairs_subset",
+    "sphx_grid_create",
     "sphx_grid_destroy", "sphx_grid_build", "sphx_grid_query", "sphx_grid_info",
     "sphx_grid_cell", "sphx_set_scenes", "sphx_get_scene_stats", "sphx_autotune",
     "sphx_density_noalloc", "sphx_set_kernel", "sphx_get_kernel", "sphx_camera_matrices",
@@ -196,6 +197,7 @@ def load_library(path: Path | str = LIB_PATH) -> C.CDLL:
         "sphx_snapshot": ([vp], C.c_int),
         "sphx_restore": ([vp], C.c_int),
         "sphx_debug_pairs": ([vp, fp, fp, C.POINTER(sz)], C.c_int),
+        "sphx_debug_pairs_subset": ([vp, sz, fp, fp, fp, C.POINTER(sz)], C.c_int),
         "sphx_density_noalloc": ([C.POINTER(SphxParams), sz, fp, fp, fp, fp, vp], C.c_int),
         "sphx_set_scenes": ([vp, C.c_uint32, fp, C.POINTER(SphxParams)], C.c_int),
         "sphx_get_scene_stats": ([vp, C.c_uint32, C.POINTER(SphxSceneStats)], C.c_int),
@@ -435,6 +437,20 @@ class Context:
 
     def restore(self):
         self._check(self._lib.sphx_restore(self._h), "sphx_restore")
+
+    def pairs_subset(self, sel) -> tuple[np.ndarray, np.ndarray]:
+        """Neighbour lists of the particles `sel` (insertion indices) only."""
+        sel = np.ascontiguousarray(sel, np.int64)
+        counts = np.zeros(sel.size, np.int64)
+        total = C.c_size_t(0)
+        f = self._lib.sphx_debug_pairs_subset
+        self._check(f(self._h, sel.size, _ptr(sel), _ptr(counts), None, C.byref(total)),
+                    "sphx_debug_pairs_subset")
+        idx = np.zeros(max(total.value, 1), np.int64)
+        total2 = C.c_size_t(total.value)
+        self._check(f(self._h, sel.size, _ptr(sel), _ptr(counts), _ptr(idx), C.byref(total2)),
+                    "sphx_debug_pairs_subset")
+        return counts, idx[: total2.value]
 
     def pairs(self) -> tuple[np.ndarray, np.ndarray]:
         """Neighbour lists of the current state: (counts[n], concatenated insertion ids)."""
