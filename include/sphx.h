@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define SPHX_ABI_VERSION 1
+#define SPHX_ABI_VERSION 2
 
 /* status codes */
 #define SPHX_OK 0
@@ -81,6 +81,8 @@ typedef struct sphx_tuning {
     int profile;           /* 1 = time each phase with CUDA events (read back lazily) */
     int graph;             /* 1 = run steps as a captured CUDA graph (recaptured when n,
                               dt, parameters or scenes change) */
+    int tile_particles;    /* particles of one cell per warp work item (tile), 1..32;
+                              0 = default (32) */
 } sphx_tuning;
 
 /* PerformanceStats (src/sph_engine.h:51-59) plus GPU-side diagnostics. */
@@ -211,11 +213,23 @@ typedef struct sphx_scene_stats {
 int sphx_get_scene_stats(sphx_ctx* ctx, uint32_t scene, sphx_scene_stats* out);
 
 /* Picks the neighbour passes' launch shape for the loaded workload: times two steps of
- * dt for each candidate (warps per CTA x resident CTAs per SM), restores the particles,
- * times and scene records after every trial, and keeps the fastest in the context.
- * Returns the choice and its time per step.  Synchronises. */
+ * dt for each candidate -- warps per CTA x resident CTAs per SM, then the tile size
+ * (particles per warp work item) at the best of those -- restores the particles, times
+ * and scene records after every trial, and keeps the fastest in the context.  Returns
+ * the launch choice and its time per step (sphx_get_tuning gives all of it).
+ * Synchronises.  No counterpart in the reference (its loops are OpenMP over particles). */
 int sphx_autotune(sphx_ctx* ctx, float dt, int* warps_per_block, int* blocks_per_sm,
                   float* best_ms);
+/* The context's current tuning (after sphx_create or sphx_autotune). */
+int sphx_get_tuning(sphx_ctx* ctx, sphx_tuning* out);
+
+/* Page-locked host memory for a caller's transfer buffers: sphx_upload reads such buffers in
+ * place over the CPU-GPU link and sphx_download fills them with the copy engines at full
+ * speed (pageable buffers go through staging copies).  The drop-in SPHEngine keeps its
+ * host mirror's transfer buffers here.  *out = NULL and SPHX_ERR_OOM when the allocation
+ * fails.  No counterpart in the reference (its particle set never leaves the host). */
+int sphx_alloc_host(void** out, size_t bytes);
+void sphx_free_host(void* ptr);
 
 /* Number of particles currently loaded. */
 int sphx_size(sphx_ctx* ctx, size_t* n);

@@ -592,6 +592,9 @@ int sphx_create(sphx_ctx** out, size_t capacity, const sphx_tuning* tuning) {
     }
     if (c->tuning.warps_per_block <= 0 || c->tuning.warps_per_block > 4)
         c->tuning.warps_per_block = kDefaultWarpsPerBlock;
+    if (c->tuning.tile_particles <= 0 || c->tuning.tile_particles > kTile)
+        c->tuning.tile_particles = kTile;
+    c->b.tile_n = c->tuning.tile_particles;
     int rc = SPHX_OK;
     auto fail = [&](int code) {
         free_all(c);
@@ -975,6 +978,31 @@ int sphx_autotune(sphx_ctx* c, float dt, int* warps_per_block, int* blocks_per_s
             bb = cd[1];
         }
     }
+    // then the tile size at the chosen launch shape
+    c->L.warps_per_block = bw;
+    c->L.blocks_per_sm = bb;
+    int bt = c->b.tile_n;
+    const int tiles[] = {16, 24};
+    for (const int tn : tiles) {
+        if (rc) break;
+        c->b.tile_n = tn;
+        if ((rc = reset()) || (rc = run_phases(c, dt, true))) break;  // warm-up
+        if ((rc = reset())) break;
+        SPHX_CUDA(cudaEventRecord(e0, c->stream));
+        if ((rc = run_phases(c, dt, true))) break;
+        if ((rc = reset())) break;
+        if ((rc = run_phases(c, dt, true))) break;
+        SPHX_CUDA(cudaEventRecord(e1, c->stream));
+        SPHX_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        SPHX_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) {
+            best = ms;
+            bt = tn;
+        }
+    }
+    c->b.tile_n = bt;
+    c->tuning.tile_particles = bt;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     c->L.warps_per_block = bw;
@@ -996,6 +1024,28 @@ int sphx_autotune(sphx_ctx* c, float dt, int* warps_per_block, int* blocks_per_s
     if (blocks_per_sm) *blocks_per_sm = bb;
     if (best_ms) *best_ms = best / 2.0f;
     return rc ? rc : rc2;
+}
+
+int sphx_get_tuning(sphx_ctx* c, sphx_tuning* out) {
+    if (!c || !out) return SPHX_ERR_INVALID_ARG;
+    *out = c->tuning;
+    return SPHX_OK;
+}
+
+int sphx_alloc_host(void** out, size_t bytes) {
+    if (!out) return SPHX_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (bytes == 0) return SPHX_ERR_INVALID_ARG;
+    if (cudaHostAlloc(out, bytes, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        *out = nullptr;
+        return SPHX_ERR_OOM;
+    }
+    return SPHX_OK;
+}
+
+void sphx_free_host(void* ptr) {
+    if (ptr) cudaFreeHost(ptr);
 }
 
 int sphx_get_scene_stats(sphx_ctx* c, uint32_t scene, sphx_scene_stats* out) {

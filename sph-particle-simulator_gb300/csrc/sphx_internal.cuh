@@ -135,6 +135,7 @@ struct Buffers {
     int radix_blocks;
     int scan_part_cap;
     int diag_blocks;
+    int tile_n = kTile;  // particles per warp work item (1 .. kTile)
 };
 constexpr uint32_t kNoSlot = 0xffffffffu;
 constexpr uint64_t kNoPairs = ~0ull;  // pair fill: this particle's list is not wanted

@@ -64,7 +64,7 @@ __device__ __forceinline__ void tile_setup(const StepConst& c, const Buffers& b,
     const uint32_t key = b.key_s[k0];
     const uint32_t end = b.off[key + 1];
     T.k0 = (int)k0;
-    T.cnt = (int)min(end - k0, (uint32_t)kTile);
+    T.cnt = (int)min(end - k0, (uint32_t)b.tile_n);
     valid = lane < T.cnt;
     xi = valid ? b.pos4_s[k0 + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
     T.cells = key < g.sentinel;
@@ -106,7 +106,7 @@ __device__ __forceinline__ void tile_setup_cells(const StepConst& c, const Buffe
     const uint32_t nc = g.sentinel;
     const uint32_t end = b.off[key + 1];
     T.k0 = (int)k0;
-    T.cnt = (int)min(end - k0, (uint32_t)kTile);
+    T.cnt = (int)min(end - k0, (uint32_t)b.tile_n);
     valid = lane < T.cnt;
     frame = b.cell4_s[k0];
     const float4 o = valid ? b.pos4_s[k0 + lane] : make_float4(0.f, 0.f, 0.f, 0.f);

@@ -243,10 +243,11 @@ struct TileSrc {
     const uint32_t* key_s;
     const uint32_t* off;
     const DevState* ds;
+    uint32_t tile_n;  // particles per tile
     __device__ bool active() const { return !ds->status; }
     __device__ uint32_t operator()(uint32_t k) const {
         const uint32_t st = off[key_s[k]];
-        return ((k - st) & (kTile - 1)) == 0 ? 1u : 0u;
+        return (k - st) % tile_n == 0 ? 1u : 0u;
     }
 };
 struct TileSink {
@@ -266,7 +267,7 @@ struct TileSink {
 };
 
 int launch_tile_scan(const LaunchCtx& L, const Buffers& b, DevState* ds, int n) {
-    return scan(L, TileSrc{b.key_s, b.off, ds}, TileSink{b.key_s, b.off, b.tile_start, ds},
+    return scan(L, TileSrc{b.key_s, b.off, ds, (uint32_t)b.tile_n}, TileSink{b.key_s, b.off, b.tile_start, ds},
          (uint32_t)n, b.scan_part, &ds->n_tiles);
 }
 

@@ -127,7 +127,10 @@ class SPHEngine {
     void sync_to_device();       // host mirror -> device, when the host changed
     void host_will_change();     // call before mutating the host mirror
 
+    float* stage() const;        // pinned transfer buffers (15 floats per particle)
+
     mutable ParticleSystem particles_;
+    mutable float* stage_ = nullptr;   // x, v, m (upload) | x, v, rho, P (download)
     SPHParameters params_;
     KernelType kernel_type_ = KernelType::CUBIC_SPLINE;
     sphx_ctx* gpu_ = nullptr;

@@ -50,32 +50,31 @@ void ParticleSystem::remove_particles(const std::vector<size_t>& indices) {
     for (size_t i = 0; i < particles_.size(); ++i) particles_[i].id = static_cast<int>(i);
 }
 
-std::vector<glm::vec3> ParticleSystem::get_positions() const {
-    std::vector<glm::vec3> out;
-    out.reserve(particles_.size());
-    for (const Particle& p : particles_) out.push_back(p.position);
+// The getters copy one field of every particle out of the AoS store (in parallel for
+// large sets: they run after every step of a host-side loop).
+template <class T, class F>
+static std::vector<T> gather(const std::vector<Particle>& ps, F field) {
+    std::vector<T> out(ps.size());
+    const long long n = static_cast<long long>(ps.size());
+#pragma omp parallel for schedule(static) if (n > 65536)
+    for (long long i = 0; i < n; ++i) out[i] = field(ps[static_cast<size_t>(i)]);
     return out;
+}
+
+std::vector<glm::vec3> ParticleSystem::get_positions() const {
+    return gather<glm::vec3>(particles_, [](const Particle& p) { return p.position; });
 }
 
 std::vector<glm::vec3> ParticleSystem::get_velocities() const {
-    std::vector<glm::vec3> out;
-    out.reserve(particles_.size());
-    for (const Particle& p : particles_) out.push_back(p.velocity);
-    return out;
+    return gather<glm::vec3>(particles_, [](const Particle& p) { return p.velocity; });
 }
 
 std::vector<float> ParticleSystem::get_densities() const {
-    std::vector<float> out;
-    out.reserve(particles_.size());
-    for (const Particle& p : particles_) out.push_back(p.density);
-    return out;
+    return gather<float>(particles_, [](const Particle& p) { return p.density; });
 }
 
 std::vector<float> ParticleSystem::get_pressures() const {
-    std::vector<float> out;
-    out.reserve(particles_.size());
-    for (const Particle& p : particles_) out.push_back(p.pressure);
-    return out;
+    return gather<float>(particles_, [](const Particle& p) { return p.pressure; });
 }
 
 void ParticleSystem::set_mass(float mass) {

@@ -50,7 +50,26 @@ SPHEngine::SPHEngine(size_t max_particles) : particles_(max_particles) {
     check(sphx_create(&gpu_, max_particles > 0 ? max_particles : 1, &t), "sphx_create");
 }
 
-SPHEngine::~SPHEngine() { sphx_destroy(gpu_); }
+SPHEngine::~SPHEngine() {
+    sphx_destroy(gpu_);
+    sphx_free_host(stage_);
+}
+
+// Page-locked transfer buffers sized for the capacity, made on first use: 7 floats per
+// particle for the upload (x, v, m: read in place by the GPU when the stream reaches the
+// upload, so they are written only after the stream went idle -- every path that changes
+// the host set downloads, and so synchronises, first) and 8 for the download (x, v, rho,
+// P).  Null when page-locked memory is not available: the transfers then go through
+// ordinary vectors.
+float* SPHEngine::stage() const {
+    if (!stage_) {
+        void* p = nullptr;
+        if (sphx_alloc_host(&p, 15 * sizeof(float) * std::max<size_t>(particles_.capacity(), 1)) ==
+            SPHX_OK)
+            stage_ = static_cast<float*>(p);
+    }
+    return stage_;
+}
 
 void SPHEngine::push_params() {
     const sphx_params p = to_sphx(params_);
@@ -117,9 +136,19 @@ void SPHEngine::host_will_change() {
 void SPHEngine::sync_to_device() {
     if (!device_dirty_) return;
     const size_t n = particles_.size();
-    std::vector<float> x(3 * n), v(3 * n), m(n);
-    for (size_t i = 0; i < n; ++i) {
-        const Particle& p = particles_[i];
+    std::vector<float> fallback;
+    float* buf = stage();
+    if (!buf) {
+        fallback.resize(7 * std::max<size_t>(n, 1));
+        buf = fallback.data();
+    }
+    float* x = buf;
+    float* v = buf + 3 * n;
+    float* m = buf + 6 * n;
+    const long long nn = static_cast<long long>(n);
+#pragma omp parallel for schedule(static) if (nn > 65536)
+    for (long long i = 0; i < nn; ++i) {
+        const Particle& p = particles_[static_cast<size_t>(i)];
         x[3 * i] = p.position.x;
         x[3 * i + 1] = p.position.y;
         x[3 * i + 2] = p.position.z;
@@ -128,7 +157,7 @@ void SPHEngine::sync_to_device() {
         v[3 * i + 2] = p.velocity.z;
         m[i] = p.mass;
     }
-    check(sphx_upload(gpu_, n, x.data(), v.data(), m.data()), "sphx_upload");
+    check(sphx_upload(gpu_, n, x, v, m), "sphx_upload");
     device_dirty_ = false;
 }
 
@@ -138,17 +167,30 @@ void SPHEngine::sync_to_device() {
 void SPHEngine::sync_to_host() const {
     if (!host_stale_) return;
     const size_t n = particles_.size();
-    std::vector<float> x(3 * n), v(3 * n), rho(n), P(n);
-    check(sphx_download(gpu_, x.data(), v.data(), rho.data(), P.data(), nullptr),
-          "sphx_download");
-    for (size_t i = 0; i < n; ++i) {
-        Particle& p = particles_[i];
+    std::vector<float> fallback;
+    float* buf = stage();
+    if (buf) {
+        buf += 7 * std::max<size_t>(particles_.capacity(), 1);  // the download region
+    } else {
+        fallback.resize(8 * std::max<size_t>(n, 1));
+        buf = fallback.data();
+    }
+    float* x = buf;
+    float* v = buf + 3 * n;
+    float* rho = buf + 6 * n;
+    float* P = buf + 7 * n;
+    check(sphx_download(gpu_, x, v, rho, P, nullptr), "sphx_download");
+    const long long nn = static_cast<long long>(n);
+    const size_t nd = densities_.size(), np = pressures_.size();
+#pragma omp parallel for schedule(static) if (nn > 65536)
+    for (long long i = 0; i < nn; ++i) {
+        Particle& p = particles_[static_cast<size_t>(i)];
         p.position = glm::vec3(x[3 * i], x[3 * i + 1], x[3 * i + 2]);
         p.velocity = glm::vec3(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
         p.density = rho[i];
         p.pressure = P[i];
-        if (i < densities_.size()) densities_[i] = rho[i];
-        if (i < pressures_.size()) pressures_[i] = P[i];
+        if (static_cast<size_t>(i) < nd) densities_[i] = rho[i];
+        if (static_cast<size_t>(i) < np) pressures_[i] = P[i];
     }
     host_stale_ = false;
 }

@@ -14,6 +14,7 @@
 #include <pybind11/pybind11.h>
 #include <pybind11/stl.h>
 
+#include <cstring>
 #include <stdexcept>
 
 #include "sph_engine.h"
@@ -23,13 +24,9 @@ namespace py = pybind11;
 namespace {
 
 py::array_t<float> vec3_array(const std::vector<glm::vec3>& v) {
+    static_assert(sizeof(glm::vec3) == 3 * sizeof(float), "glm::vec3 is three packed floats");
     py::array_t<float> out({static_cast<py::ssize_t>(v.size()), static_cast<py::ssize_t>(3)});
-    auto m = out.mutable_unchecked<2>();
-    for (size_t i = 0; i < v.size(); ++i) {
-        m(i, 0) = v[i].x;
-        m(i, 1) = v[i].y;
-        m(i, 2) = v[i].z;
-    }
+    if (!v.empty()) std::memcpy(out.mutable_data(), v.data(), v.size() * sizeof(glm::vec3));
     return out;
 }
 

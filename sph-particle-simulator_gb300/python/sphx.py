@@ -45,7 +45,8 @@ EXPORTS = (
     "sphx_grid_create",
     "sphx_grid_destroy", "sphx_grid_build", "sphx_grid_query", "sphx_grid_info",
     "sphx_grid_cell", "sphx_set_scenes", "sphx_get_scene_stats", "sphx_autotune",
-    "sphx_density_noalloc", "sphx_set_kernel", "sphx_get_kernel", "sphx_camera_matrices",
+    "sphx_density_noalloc", "sphx_get_tuning", "sphx_alloc_host", "sphx_free_host",
+    "sphx_set_kernel", "sphx_get_kernel", "sphx_camera_matrices",
     "sphx_render_instances", "sphx_render_instances_device", "sphx_render_image",
     "sphx_render_image_device", "sphx_generate", "sphx_generate_scene",
 )
@@ -61,7 +62,8 @@ class SphxParams(C.Structure):
 
 class SphxTuning(C.Structure):
     _fields_ = [("mode", C.c_int), ("warps_per_block", C.c_int), ("blocks_per_sm", C.c_int),
-                ("max_grid_cells", C.c_int64), ("profile", C.c_int), ("graph", C.c_int)]
+                ("max_grid_cells", C.c_int64), ("profile", C.c_int), ("graph", C.c_int),
+                ("tile_particles", C.c_int)]
 
 
 class SphxSceneStats(C.Structure):
@@ -201,6 +203,7 @@ def load_library(path: Path | str = LIB_PATH) -> C.CDLL:
         "sphx_density_noalloc": ([C.POINTER(SphxParams), sz, fp, fp, fp, fp, vp], C.c_int),
         "sphx_set_scenes": ([vp, C.c_uint32, fp, C.POINTER(SphxParams)], C.c_int),
         "sphx_get_scene_stats": ([vp, C.c_uint32, C.POINTER(SphxSceneStats)], C.c_int),
+        "sphx_get_tuning": ([vp, C.POINTER(SphxTuning)], C.c_int),
         "sphx_autotune": ([vp, C.c_float, C.POINTER(C.c_int), C.POINTER(C.c_int),
                            C.POINTER(C.c_float)], C.c_int),
         "sphx_grid_create": ([C.POINTER(vp), sz], C.c_int),
@@ -248,11 +251,11 @@ class Context:
 
     def __init__(self, capacity: int, *, mode: int = MODE_EXACT, warps_per_block: int = 0,
                  blocks_per_sm: int = 0, max_grid_cells: int = 0, profile: bool = False,
-                 graph: bool = False):
+                 graph: bool = False, tile_particles: int = 0):
         self._lib = lib()
         self._h = C.c_void_p()
         t = SphxTuning(mode, warps_per_block, blocks_per_sm, max_grid_cells, int(profile),
-                       int(graph))
+                       int(graph), tile_particles)
         self._check(self._lib.sphx_create(C.byref(self._h), capacity, C.byref(t)), "sphx_create")
         self.capacity = capacity
 
@@ -367,6 +370,12 @@ class Context:
         self._check(self._lib.sphx_autotune(self._h, C.c_float(dt), C.byref(w), C.byref(b),
                                             C.byref(ms)), "sphx_autotune")
         return w.value, b.value, ms.value
+
+    def tuning(self) -> dict:
+        """The context's launch shape and options (after creation or autotune)."""
+        t = SphxTuning()
+        self._check(self._lib.sphx_get_tuning(self._h, C.byref(t)), "sphx_get_tuning")
+        return {name: getattr(t, name) for name, _ in t._fields_}
 
     def scene_stats(self, scene: int) -> dict:
         st = SphxSceneStats()

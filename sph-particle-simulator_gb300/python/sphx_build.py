@@ -77,7 +77,7 @@ def build_sphx(force: bool = False) -> Path:
 
 
 HOST_SOURCES = ["kernels.cpp", "particle.cpp", "spatial_hash.cpp", "sph_engine.cpp"]
-HOST_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
+HOST_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fopenmp", "-Wall", "-Wextra",
               f"-I{REPO / 'include'}", f"-I{PKG / 'host' / 'include'}",
               "-idirafter", str(PKG / "host" / "compat")]
 

@@ -32,7 +32,7 @@ def test_library_exports_every_declared_symbol(built):
 
 def test_version_and_error_strings(built):
     lib = sphx.lib()
-    assert lib.sphx_version() == 1
+    assert lib.sphx_version() == 2
     for code in range(-8, 1):
         assert lib.sphx_strerror(code)
 
@@ -41,7 +41,7 @@ def test_struct_layouts_match_header():
     # 16 floats in SPHParameters order; fixed-width stats record
     assert C.sizeof(sphx.SphxParams) == 64
     assert [f for f, _ in sphx.SphxParams._fields_][-1] == "neighbor_search_radius"
-    assert C.sizeof(sphx.SphxTuning) == 32  # 5 ints + int64, padded
+    assert C.sizeof(sphx.SphxTuning) == 40  # 6 ints + int64, padded
     assert C.sizeof(sphx.SphxStats) == 5 * 8 + 3 * 8 + 2 * 4 + 4 * 4 + 7 * 8 + 8
 
 

@@ -91,6 +91,7 @@ def test_autotune_keeps_state_and_results():
     ctx.set_scenes(b.scene_start, b.params)
     w, bps, ms = ctx.autotune(5e-4)
     assert w in (1, 2, 4) and ms > 0
+    assert ctx.tuning()["tile_particles"] in (16, 24, 32)
     assert np.array_equal(ctx.download(vel=False, rho=False, pressure=False, acc=False)["pos"], b.pos)
     ctx.step(5e-4)
     tuned = ctx.download(acc=False)

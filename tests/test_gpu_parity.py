@@ -277,3 +277,20 @@ def test_gpu_huge_box_folds_the_grid(port, max_cells):
     st = ctx.stats()
     if max_cells:
         assert st["grid_cells"] <= max(max_cells, 125)
+
+
+@pytest.mark.parametrize("tile", [7, 16, 24])
+def test_gpu_tile_sizes_keep_every_field_bit_exact(port, tile):
+    """Tiles of fewer particles per warp work item (a tuning choice) change only how the
+    work is split: one step stays bit-identical to the oracle."""
+    w = I.scaled_dam_break(60_000, seed=17)
+    ctx = make_ctx(w.n, w.params, w.pos, w.vel, w.mass, tile_particles=tile)
+    assert ctx.tuning()["tile_particles"] == tile
+    ctx.step(w.dt)
+    e = O.Engine(port, w.n)
+    e.initialize(w.params)
+    e.add(w.pos, w.vel, w.mass)
+    e.step(w.dt)
+    out, ref = ctx.download(), e.get()
+    for k in ("pos", "vel", "rho", "pressure", "acc"):
+        assert_bits(out[k], ref[k], k)
