@@ -26,10 +26,14 @@ describes.  Between timed steps the L2 cache is flushed (a 512 MiB buffer is wri
              the kernel time, against SMs x 4 issue slots per clock x the sampled SM clock
   cpu_baseline  the oracle port (C restatement of the reference step, OpenMP on all host
              cores) on a bounded sample of the same workload
-  extras     batched_256 (the 256-scene mix, batched vs looped plain steps), dam_break_10M
-             (exact and precision mode, fresh-state), dam_break_1M_faithful (the workload's
-             own trajectory with per-step cell occupancy and non-finite counts, bounded to
-             30 s of device time)
+  extras     e2e_dropin (sph.Simulator step + get_positions + get_densities, host clock),
+             batched_256 (the 256-scene mix, batched vs looped plain steps, autotuned, with
+             its own trajectory bounded to 30 s and an FP64 density check of 8 scenes in the
+             CPU leg), dam_break_10M (exact and precision mode, fresh-state),
+             dam_break_10M_trajectory (the 10M configuration's own 50 CFL steps in precision
+             mode with per-step FP64 mass / energy drift, bounded to 60 s of device time),
+             dam_break_1M_faithful (the 1M workload's own trajectory with per-step cell
+             occupancy and non-finite counts, bounded to 30 s of device time)
 
 --impl reference times the reference's CPU implementation of the path (the oracle port:
 the reference's own build cannot be compiled on the GPU host) on all host cores, on the
@@ -216,6 +220,17 @@ def run_cpu(w: I.Workload, steps: int, warmup: int, budget_s: float | None = Non
             "sample": f"{w.name}: {w.n} particles, {len(times)} fresh-state steps"}
 
 
+def workload_config(w: I.Workload, workload_name: str, world: int) -> dict:
+    """The `config` object of both arms' JSON lines: the workload and its protocol."""
+    return {
+        "workload": workload_name, "particles": w.n,
+        "lattice": "x".join(map(str, w.info.get("lattice", ()))), "dt": w.dt,
+        "protocol": "fresh-state (initial state restored before each step)",
+        "l2": "GPU arm: flushed between timed steps (512 MiB write)", "mode": "exact",
+        "parallelism": f"replicas x{world}",
+    }
+
+
 def bench_reference(args, world, rank):
     if rank != 0:
         return 0
@@ -228,8 +243,8 @@ def bench_reference(args, world, rank):
         "ms_per_step": 1e3 * r["seconds"] / max(r["steps"], 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": r["value"] / PUBLISHED_1M if args.workload == "dam_break_1M" else None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "particles": w.n, "protocol": "fresh-state",
-                   "dt": w.dt, "implementation": "oracle port of the reference step (C, OpenMP)"},
+        "config": workload_config(w, args.workload, world),
+        "implementation": "oracle port of the reference step (C, OpenMP on all host cores)",
         "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": "port",
                          "sample": r["sample"]},
         "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -279,7 +294,13 @@ def bench_batched(torch, stream, flush, steps):
         ctx.step(b.dt)
     ms = timed_steps(torch, ctx, b, steps, flush)
     batched_ms = sum(ms) / steps
-    launches_per_step = None
+    tuned = ctx.tuning()
+    # the densities of one batched step from the initial state, for the FP64 check of the
+    # CPU leg (sampled scenes)
+    ctx.restore()
+    ctx.step(b.dt)
+    rho_batched = ctx.download(pos=False, vel=False, pressure=False, acc=False)["rho"]
+    traj = bench_batched_trajectory(torch, ctx, b)
     ctx.close()
     ctxs = []
     for s in range(len(b.params)):
@@ -311,9 +332,155 @@ def bench_batched(torch, stream, flush, steps):
             "batched_value": b.n / (batched_ms * 1e-3), "batched_ms_per_step": batched_ms,
             "looped_plain_value": b.n / (looped_ms * 1e-3), "looped_ms_per_step": looped_ms,
             "speedup": looped_ms / batched_ms, "unit": UNIT,
-            "autotuned": {"warps_per_block": wpb, "blocks_per_sm": bps, "ms": tuned_ms},
+            "autotuned": {"warps_per_block": wpb, "blocks_per_sm": bps,
+                          "tile_particles": tuned["tile_particles"],
+                          "threads_per_tile": 32, "cell_size_multiplier": 1, "ms": tuned_ms},
+            "trajectory": traj,
             "protocol": "fresh-state, dt 5e-4, exact mode (every scene bit-identical to "
-                        "stepping it alone), batched step captured as a CUDA graph"}
+                        "stepping it alone), batched step captured as a CUDA graph"}, rho_batched
+
+
+def bench_batched_trajectory(torch, ctx, b, budget_s=30.0):
+    """The batched mix's own trajectory: up to its 200 steps at dt 5e-4 from the initial
+    state, batched and graph-replayed, each step timed on the device, with the FP64 mass
+    and energy summed over the scenes after every step.  Stops after the step crossing
+    `budget_s` of device time (the drops' dynamics crowd the cells within a few steps)."""
+    ctx.restore()
+    torch.cuda.synchronize()
+    mass0 = float(b.mass.astype(np.float64).sum())
+    log, total = [], 0.0
+    for s in range(b.steps):
+        e_a, e_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e_a.record()
+        ctx.step(b.dt)
+        e_b.record()
+        torch.cuda.synchronize()
+        ms = e_a.elapsed_time(e_b)
+        st = ctx.stats()
+        mass, energy = 0.0, 0.0
+        for k in range(len(b.params)):
+            sc = ctx.scene_stats(k)
+            mass += sc["sum_mass"]
+            energy += sc["kinetic_energy"] + sc["potential_energy"]
+        log.append([round(ms, 3), (mass - mass0) / mass0, energy, st["max_cell_occupancy"]])
+        total += ms * 1e-3
+        if total > budget_s:
+            break
+    return {"steps_done": len(log), "steps": b.steps, "dt": b.dt, "device_s": total,
+            "value": b.n * len(log) / total, "unit": UNIT, "per_step": log,
+            "per_step_fields": ["ms", "mass_drift_rel", "fp64_energy_sum",
+                                "max_cell_occupancy"],
+            "protocol": f"faithful batched trajectory from the initial state, stopped after "
+                        f"the step crossing {budget_s:.0f} s of device time"}
+
+
+def batched_fp64_check(port, rho_batched, nsample=8):
+    """Density relative error of the batched step against the oracle's FP64 re-evaluation
+    of the same initial state, on a seeded sample of scenes (the CPU leg's checker)."""
+    b = I.batched_fluid_drops()
+    rng = np.random.default_rng(33)
+    worst, means = 0.0, []
+    picked = sorted(int(x) for x in rng.choice(len(b.params), nsample, replace=False))
+    for s in picked:
+        pos, vel, mass, prm = b.scene(s)
+        a, e = int(b.scene_start[s]), int(b.scene_start[s + 1])
+        rho64, _, _ = port.fields_f64(pos, vel, mass, prm)
+        rel = np.abs(rho_batched[a:e].astype(np.float64) - rho64) / np.abs(rho64)
+        worst = max(worst, float(rel.max()))
+        means.append(float(rel.mean()))
+    return {"fp64_rho_rel_max": worst, "fp64_rho_rel_mean": float(np.mean(means)),
+            "fp64_scenes_checked": picked}
+
+
+def bench_10m_trajectory(torch, stream, w10, budget_s=60.0):
+    """The 10M dam break as its configuration states it: from the initial state, up to its
+    50 steps with step(0) (CFL timestep, FP64 maximum, capped at params.timestep = 2e-4) in
+    the precision mode, each step timed on the device, with the FP64 mass, momentum and
+    energy (kinetic + gravitational potential) after every step and their drift from the
+    initial state's (summed in FP64 on the host from the inputs).  Stops after the step
+    that crosses `budget_s` of device time."""
+    import sphx
+
+    ctx = sphx.Context(w10.n, mode=sphx.MODE_PRECISE)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_params(w10.params)
+    ctx.upload(w10.pos, w10.vel, w10.mass)
+    m64 = w10.mass.astype(np.float64)
+    g = float(w10.params[6])
+    mass0 = float(m64.sum())
+    e0 = float((0.5 * m64 * (w10.vel.astype(np.float64) ** 2).sum(1)).sum()
+               + (-m64 * g * w10.pos[:, 1].astype(np.float64)).sum())
+    torch.cuda.synchronize()
+    log, total = [], 0.0
+    for s in range(w10.steps):
+        e_a, e_b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e_a.record()
+        ctx.step(0.0)
+        e_b.record()
+        torch.cuda.synchronize()
+        ms = e_a.elapsed_time(e_b)
+        st = ctx.stats()
+        t, dt = ctx.time_f64()
+        energy = st["kinetic_energy"] + st["potential_energy"]
+        log.append([round(ms, 3), dt, t, (st["sum_mass"] - mass0) / mass0,
+                    (energy - e0) / abs(e0), st["momentum"][0], st["momentum"][1],
+                    st["momentum"][2], st["max_cell_occupancy"], st["nonfinite_particles"]])
+        total += ms * 1e-3
+        if total > budget_s:
+            break
+    ctx.close()
+    done = len(log)
+    return {"value": w10.n * done / total, "unit": UNIT, "steps_done": done,
+            "steps": w10.steps, "device_s": total, "mode": "cell + FP32 offset, compensated sums",
+            "initial_fp64_mass": mass0, "initial_fp64_energy": e0,
+            "max_abs_mass_drift": max(abs(r[3]) for r in log),
+            "final_energy_drift": log[-1][4], "per_step": log,
+            "per_step_fields": ["ms", "dt_fp64", "time_fp64", "mass_drift_rel",
+                                "energy_drift_rel", "momentum_x", "momentum_y", "momentum_z",
+                                "max_cell_occupancy", "nonfinite_particles"],
+            "protocol": f"faithful trajectory from the initial state, step(0) (CFL, FP64 max, "
+                        f"cap 2e-4), stopped after the step crossing {budget_s:.0f} s of "
+                        f"device time"}
+
+
+def bench_dropin(w, steps):
+    """The drop-in engine end to end, as a user of the reference's Python API drives it:
+    sph.Simulator (the C++ SPHEngine over the C ABI) -- step(dt), then get_positions() and
+    get_densities() -- host wall clock per step.  The particle set is restored before
+    every step (clear_particles + add_particles_array, outside the timed interval), so
+    each step uploads its inputs from the host mirror (x, v, m) inside step() and the
+    getters download x, v, rho and P into the mirror and copy them out."""
+    lib = REPO / "sph-particle-simulator_gb300" / "lib"
+    if str(lib) not in sys.path:
+        sys.path.insert(0, str(lib))
+    import sph
+
+    prm = w.params
+    p = sph.SPHParameters()
+    (p.rest_density, p.gas_constant, p.viscosity, p.smoothing_length, p.particle_mass,
+     p.timestep, p.gravity, p.damping, p.CFL_factor) = (float(x) for x in prm[:9])
+    p.bounds = [float(x) for x in prm[9:15]]
+    p.neighbor_search_radius = float(prm[15])
+    sim = sph.Simulator(w.n)
+    sim.initialize(p)
+    times = []
+    for k in range(steps + 2):
+        sim.clear_particles()
+        sim.add_particles_array(w.pos, w.vel, w.mass)
+        t0 = time.perf_counter()
+        sim.step(w.dt)
+        x = sim.get_positions()
+        rho = sim.get_densities()
+        t1 = time.perf_counter()
+        if k >= 2:
+            times.append(t1 - t0)
+    med = statistics.median(times)
+    return {"value": w.n / med, "unit": UNIT, "steps": steps, "ms_per_step_median": 1e3 * med,
+            "ms_per_step_min": 1e3 * min(times), "h2d_bytes_per_step": 28 * w.n,
+            "d2h_bytes_per_step": 40 * w.n,
+            "rho_mean": float(np.mean(rho[: w.n])), "x_mean": float(np.mean(x)),
+            "path": "sph.Simulator.step + get_positions + get_densities (pybind11 module over "
+                    "the C++ drop-in SPHEngine, libsph_gb300.so -> libsphx.so)"}
 
 
 def bench_10m_precise(torch, stream, flush, w10, steps):
@@ -483,9 +650,14 @@ def bench_ours(args, world, rank, local):
 
     # secondary workloads (device-timed): the 10M dam break and the batched scene mix
     extra = {}
+    rho_batched = None
+    if not args.no_dropin:
+        ctx.close()
+        extra["e2e_dropin"] = bench_dropin(w, max(3, min(args.steps, 10)))
     if args.workload == "dam_break_1M" and not args.no_batch:
         ctx.close()
-        extra["batched_256"] = bench_batched(torch, stream, flush, max(3, min(args.steps, 10)))
+        extra["batched_256"], rho_batched = bench_batched(torch, stream, flush,
+                                                          max(3, min(args.steps, 10)))
     if args.workload == "dam_break_1M" and not args.no_10m:
         w10 = workload("dam_break_10M")
         ctx.close()
@@ -513,6 +685,7 @@ def bench_ours(args, world, rank, local):
         }
         ctx10.close()
         extra["dam_break_10M_precise"] = bench_10m_precise(torch, stream, flush, w10, k10)
+        extra["dam_break_10M_trajectory"] = bench_10m_trajectory(torch, stream, w10)
     elif not ctx_closed(ctx):
         ctx.close()
     if args.workload == "dam_break_1M" and not args.no_faithful:
@@ -548,22 +721,20 @@ def bench_ours(args, world, rank, local):
     cpu = None
     if world == 1 and not args.no_cpu:
         cpu = run_cpu(w, steps=8, warmup=0, budget_s=15.0)
+        if rho_batched is not None:  # the oracle as the checker of the batched densities
+            import sph_oracle as O
+
+            extra["batched_256"].update(batched_fp64_check(O.Port(), rho_batched))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * dev_s / args.steps,
         "higher_is_better": True, "scaling": "weak",
         "vs_baseline": value / PUBLISHED_1M if args.workload == "dam_break_1M" else None,
         "dtype": "f32", "data": "synthetic",
-        "config": {
-            "workload": args.workload, "particles": w.n,
-            "lattice": "x".join(map(str, w.info.get("lattice", ()))), "dt": w.dt,
-            "protocol": "fresh-state (initial state restored on the device before each step)",
-            "l2": "flushed between timed steps (512 MiB write)", "mode": "exact",
-            "launch": "step captured as a CUDA graph and replayed (sphx_tuning.graph); "
-                      "eager launches: %.4f ms/step" % (sum(ms_eager) / args.steps),
-            "parallelism": f"replicas x{world}",
-            "vs_baseline_ref": "README.md:45 CPU 1M 38 steps/s = 3.8e7 particle-steps/s",
-        },
+        "config": workload_config(w, args.workload, world),
+        "launch": "step captured as a CUDA graph and replayed (sphx_tuning.graph); "
+                  "eager launches: %.4f ms/step" % (sum(ms_eager) / args.steps),
+        "vs_baseline_ref": "README.md:45 CPU 1M 38 steps/s = 3.8e7 particle-steps/s",
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 28 * w.n,
                 "d2h_bytes_per_step": 28 * w.n,
                 "path": "sphx_upload (pinned) + sphx_step + sphx_download (pos, vel, rho)"},
@@ -607,6 +778,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-scene figure")
     ap.add_argument("--no-faithful", action="store_true",
                     help="skip the faithful-trajectory figure")
+    ap.add_argument("--no-dropin", action="store_true",
+                    help="skip the drop-in engine's end-to-end figure")
     args = ap.parse_args()
     world, rank, local = dist_env()
     if args.impl == "reference":

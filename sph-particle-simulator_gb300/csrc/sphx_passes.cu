@@ -400,14 +400,20 @@ __device__ __forceinline__ uint32_t chunk_hits_x2(const float* cx, const float* 
     return mask;
 }
 
-// W(q) in precision mode (same formula, contracted arithmetic)
-__device__ __forceinline__ float cubic_w_p(const StepConst& c, float q) {
-    if (q <= 1.0f) return c.sigma * (2.0f / 3.0f - q * q + 0.5f * q * q * q);
-    if (q <= 2.0f) {
-        const float t = 2.0f - q;
-        return c.sigma * (t * t * t * (1.0f / 6.0f));
-    }
-    return 0.0f;
+// |r| and 1/|r| of a pair from d2 = |r|^2 with the hardware reciprocal square root (a few
+// ulp): precision mode only.  A coincident pair (d2 = 0) gets |r| = 0 and 1/|r| = 0.
+__device__ __forceinline__ void fast_len(float d2, float& r, float& rinv) {
+    rinv = d2 > 0.0f ? rsqrtf(d2) : 0.0f;
+    r = d2 * rinv;
+}
+
+// W(q) in precision mode: the same formula with contracted arithmetic, both branches
+// evaluated and one selected (q of a hit is at most 2 up to rounding)
+__device__ __forceinline__ float cubic_w_fast(const StepConst& c, float q) {
+    const float t = 2.0f - q;
+    const float w1 = c.sigma * fmaf(q * q, fmaf(0.5f, q, -1.0f), 2.0f / 3.0f);
+    const float w2 = c.sigma * (1.0f / 6.0f) * (t * t * t);
+    return q <= 1.0f ? w1 : (q <= 2.0f ? w2 : 0.0f);
 }
 
 // W of the pair (x_i - x_j = (dx, dy, dz), d2 = |.|^2) for smoothing kernel K.
@@ -422,16 +428,20 @@ __device__ __forceinline__ float pair_w_exact(const StepConst& c, float d2) {
                         : xdiv_fixed(xsqrt(d2), c.h, c.rcp_h, c.fast_div_h);
     return K == SPHX_KERNEL_WENDLAND_C2 ? wendland_w(c, q) : cubic_w(c, q);
 }
+// W of a pair in precision mode: contracted arithmetic, hardware reciprocal square root
+// and exponential (errors of a few ulp per term, far inside the stated bounds)
 template <int K>
-__device__ __forceinline__ float pair_w_p(const StepConst& c, float d2) {
-    if (K == SPHX_KERNEL_GAUSSIAN) return c.wnorm * expf(-d2 * c.gs);
-    const float q = sqrtf(d2) / c.h;
+__device__ __forceinline__ float pair_w_fast(const StepConst& c, float d2) {
+    if (K == SPHX_KERNEL_GAUSSIAN) return c.wnorm * __expf(-d2 * c.gs);
+    float r, rinv;
+    fast_len(d2, r, rinv);
+    const float q = r * c.rcp_h;
     if (K == SPHX_KERNEL_WENDLAND_C2) {
-        if (q >= 2.0f) return 0.0f;
-        const float t = 1.0f - 0.5f * q;
-        return c.wnorm * (t * t) * (t * t) * (2.0f * q + 1.0f);
+        const float t = fmaf(-0.5f, q, 1.0f);
+        const float t2 = t * t;
+        return q < 2.0f ? c.wnorm * (t2 * t2) * fmaf(2.0f, q, 1.0f) : 0.0f;
     }
-    return cubic_w_p(c, q);
+    return cubic_w_fast(c, q);
 }
 
 // Work distribution: warps take tiles from a per-pass counter (dynamic, so crowded cells
@@ -461,7 +471,7 @@ struct DensitySmem {
 };
 
 template <bool kPrecise, bool kBatch, int kKern, bool kNZ>
-__global__ void __launch_bounds__(128, 10) k_density(const StepConst cp, const Buffers b,
+__global__ void __launch_bounds__(128, kPrecise ? 9 : 10) k_density(const StepConst cp, const Buffers b,
                                                  DevState* ds) {
     if (ds->status) return;
     extern __shared__ __align__(16) unsigned char smem_raw_d[];
@@ -545,13 +555,35 @@ __global__ void __launch_bounds__(128, 10) k_density(const StepConst cp, const B
                 if (rec) __stcs(rec, mask);
                 nn += __popc(mask);
                 const int self = i - s;
-                if ((unsigned)self < 32u) mask &= ~(1u << self);
+                const uint32_t selfbit = (unsigned)self < 32u ? 1u << self : 0u;
+                mask &= ~selfbit;
+                // dense chunk (collapsed cells): every particle of the tile hits every
+                // candidate but itself; each lane adds its own terms in candidate order --
+                // the flattened path's terms and additions, without the hit list and the
+                // lane-by-lane fold
+                const uint32_t all_m = m == 32 ? kFull : (1u << m) - 1u;
+                if (__all_sync(kFull, !valid || mask == (all_m & ~selfbit))) {
+                    float part = 0.0f;
+                    for (int jj = 0; jj < m; ++jj) {
+                        if (!valid || jj == self) continue;
+                        const float4 xj = S->cand[jj];
+                        if (kPrecise) {
+                            const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+                            part += xj.w * pair_w_fast<kKern>(c, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+                        } else {
+                            rho = xadd(rho, xmul(xj.w, pair_w_exact<kKern, kNZ>(c, diff_d2(xi, xj))));
+                        }
+                    }
+                    if (kPrecise) rk.add(part);
+                    continue;
+                }
                 const uint32_t cnt = __popc(mask);
                 uint32_t H;
                 const uint32_t o = warp_excl_scan(cnt, lane, H);
                 if (!H) continue;
                 list_hits(S->plist, mask, o, lane);
                 __syncwarp();
+                float part = 0.0f;  // precision mode: this chunk's terms, one FP32 sum
                 for (uint32_t base = 0; base < H; base += kDensityBatch) {
                     const uint32_t end = min(H, base + kDensityBatch);
                     for (uint32_t f = base + lane; f < end; f += 32) {
@@ -560,7 +592,8 @@ __global__ void __launch_bounds__(128, 10) k_density(const StepConst cp, const B
                         if (kPrecise) {
                             const float4 xt = S->tpos[pr >> 5];
                             const float dx = xt.x - xj.x, dy = xt.y - xj.y, dz = xt.z - xj.z;
-                            S->tbuf[f - base] = xj.w * pair_w_p<kKern>(c, dx * dx + dy * dy + dz * dz);
+                            S->tbuf[f - base] =
+                                xj.w * pair_w_fast<kKern>(c, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
                         } else {
                             const float d2 = diff_d2(S->tpos[pr >> 5], xj);
                             S->tbuf[f - base] = xmul(xj.w, pair_w_exact<kKern, kNZ>(c, d2));
@@ -569,11 +602,12 @@ __global__ void __launch_bounds__(128, 10) k_density(const StepConst cp, const B
                     __syncwarp();
                     const uint32_t k1 = min(o + cnt, end);
                     if (kPrecise)
-                        for (uint32_t k = max(o, base); k < k1; ++k) rk.add(S->tbuf[k - base]);
+                        for (uint32_t k = max(o, base); k < k1; ++k) part += S->tbuf[k - base];
                     else
                         for (uint32_t k = max(o, base); k < k1; ++k) rho = xadd(rho, S->tbuf[k - base]);
                     __syncwarp();
                 }
+                if (kPrecise) rk.add(part);  // compensated across chunks
             }
         }
         if (b.hitmask && lane == 0) {
@@ -606,6 +640,19 @@ __global__ void __launch_bounds__(128, 10) k_density(const StepConst cp, const B
 __device__ __forceinline__ float4 stage_aux(float4 a, float visc) {
     a.w = xmul(a.w, visc);
     return a;
+}
+
+// Precision mode: a candidate's factors of the fast pair term, formed once per staged
+// candidate from (rho, P, 2 rho, m / rho): m_j / (2 rho_j), m_j P_j / (2 rho_j) and
+// (m_j / rho_j) mu, so that the pressure factor m_j (P_t + P_j) / (2 rho_j) is one FMA.
+__device__ __forceinline__ float4 stage_aux_fast(float4 a, float visc) {
+    const float half_mr = 0.5f * a.w;
+    return make_float4(half_mr, half_mr * a.y, a.w * visc, 0.0f);
+}
+
+template <bool kPrecise>
+__device__ __forceinline__ float4 stage_aux_t(float4 a, float visc) {
+    return kPrecise ? stage_aux_fast(a, visc) : stage_aux(a, visc);
 }
 
 struct ForceSmem {
@@ -759,47 +806,47 @@ __device__ __forceinline__ void force_term_cubic_x2(const StepConst& c, const fl
     B = make_float2(pz, vz);
 }
 
-// Precision-mode pair term: the same formulas with contracted FP32 arithmetic.
+// Precision-mode pair term: the pressure and viscosity contributions of candidate j to the
+// force on particle t, summed into one vector (the mode is judged against FP64, not against
+// the reference's summation order), with contracted FP32 arithmetic, the hardware
+// reciprocal square root and exponential, and the per-candidate factors of
+// stage_aux_fast in aj.  Formulas: equations::compute_pressure_force /
+// compute_viscosity_force (sph_engine.cpp:390-432) with grad W = g * r_vec and
+// laplacian W = lap of the kernel; the pressure term is skipped for |r| < 1e-6.
 template <int K>
-__device__ __forceinline__ void force_term_p(const StepConst& c, const float4& xt,
-                                             const float4& vt, float Pt, const float4& xj,
-                                             const float4& vj, const float4& aj, float* p3,
-                                             float* v3) {
+__device__ __forceinline__ float3 force_term_fast(const StepConst& c, const float4& xt,
+                                                  const float4& vt, float Pt, const float4& xj,
+                                                  const float4& vj, const float4& aj) {
     const float dx = xt.x - xj.x, dy = xt.y - xj.y, dz = xt.z - xj.z;
-    const float d2 = dx * dx + dy * dy + dz * dz;
-    const float r_len = sqrtf(d2);
-    const float q = r_len / c.h;
-    const bool skip = r_len < 1e-6f;
-    p3[0] = p3[1] = p3[2] = 0.0f;
-    float g = 0.0f, lap = 0.0f;  // grad W = g * r
+    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    float r, rinv;
+    fast_len(d2, r, rinv);
+    float g, lap;
     if (K == SPHX_KERNEL_GAUSSIAN) {
-        const float e = expf(-d2 * c.gs);
+        const float e = __expf(-d2 * c.gs);
         g = c.gg * e;
-        lap = c.gl * e * (c.g2s * d2 - 3.0f);
-    } else if (K == SPHX_KERNEL_WENDLAND_C2) {
-        if (q < 2.0f) {
-            const float t = 1.0f - 0.5f * q;
-            g = c.wnorm * (-5.0f * t * t * t * q) / (r_len * c.h);
-            lap = c.wl * t * t * (5.0f * q - 3.0f);
-        }
+        lap = c.gl * e * fmaf(c.g2s, d2, -3.0f);
     } else {
-        float gf = 0.0f;
-        if (q <= 1.0f) gf = c.sigma * (-2.0f * q + 1.5f * q * q);
-        else if (q <= 2.0f) gf = -c.sigma * 0.5f * (2.0f - q) * (2.0f - q);
-        g = gf / (r_len * c.h);
-        if (q <= 1.0f) lap = c.sigma * (-2.0f + 3.0f * q) / c.h_sq;
-        else if (q <= 2.0f) lap = c.sigma * (2.0f - q) / c.h_sq;
+        const float q = r * c.rcp_h;
+        if (K == SPHX_KERNEL_WENDLAND_C2) {
+            const float t = fmaf(-0.5f, q, 1.0f);
+            const bool in = q < 2.0f;
+            g = in ? c.wnorm * (-5.0f * (t * t * t) * q) * (rinv * c.rcp_h) : 0.0f;
+            lap = in ? c.wl * (t * t) * fmaf(5.0f, q, -3.0f) : 0.0f;
+        } else {
+            const float t = 2.0f - q;
+            const float gf = q <= 1.0f ? c.sigma * q * fmaf(1.5f, q, -2.0f)
+                                       : (q <= 2.0f ? -0.5f * c.sigma * (t * t) : 0.0f);
+            g = gf * (rinv * c.rcp_h);
+            const float sh = c.sigma * c.rcp_hsq;
+            lap = q <= 1.0f ? sh * fmaf(3.0f, q, -2.0f) : (q <= 2.0f ? sh * t : 0.0f);
+        }
     }
-    if (!skip) {
-        const float s = xj.w * (Pt + aj.y) / aj.z * g;
-        p3[0] = s * dx;
-        p3[1] = s * dy;
-        p3[2] = s * dz;
-    }
-    const float sv = aj.w * lap;  // aj.w = (m_j / rho_j) * mu
-    v3[0] = sv * (vj.x - vt.x);
-    v3[1] = sv * (vj.y - vt.y);
-    v3[2] = sv * (vj.z - vt.z);
+    if (r < 1e-6f) g = 0.0f;
+    const float cp = -fmaf(Pt, aj.x, aj.y) * g;  // -(m_j (P_t + P_j) / (2 rho_j)) g
+    const float cv = aj.z * lap;                  // (m_j / rho_j) mu lap
+    return make_float3(fmaf(cp, dx, cv * (vj.x - vt.x)), fmaf(cp, dy, cv * (vj.y - vt.y)),
+                       fmaf(cp, dz, cv * (vj.z - vt.z)));
 }
 
 // Precision-mode leapfrog + wall clamp on cell + offset positions (FP64 clamp).
@@ -843,7 +890,7 @@ __device__ __forceinline__ void integrate_cells(const StepConst& c, float dt, co
 }
 
 template <bool kIntegrate, bool kPrecise, bool kBatch, int kKern, bool kNZ>
-__global__ void __launch_bounds__(128, 7) k_force(const StepConst cp, const Buffers b,
+__global__ void __launch_bounds__(128, kPrecise ? 6 : 7) k_force(const StepConst cp, const Buffers b,
                                                DevState* ds) {
     if (ds->status) return;
     extern __shared__ __align__(16) unsigned char smem_raw_f[];
@@ -905,7 +952,7 @@ __global__ void __launch_bounds__(128, 7) k_force(const StepConst cp, const Buff
                         if (kPrecise) pl = frame_pos(b.cell4_s[s + lane], frame, pl, c.cs);
                         S->cpos[lane] = pl;
                         S->cvel[lane] = b.vel4_s[s + lane];
-                        S->caux[lane] = stage_aux(b.aux4_s[s + lane], c.visc);
+                        S->caux[lane] = stage_aux_t<kPrecise>(b.aux4_s[s + lane], c.visc);
                     }
                     __syncwarp();
                 } else {
@@ -922,7 +969,7 @@ __global__ void __launch_bounds__(128, 7) k_force(const StepConst cp, const Buff
                     if (!surv) continue;
                     if (surv & (1u << lane)) {
                         S->cvel[lane] = b.vel4_s[s + lane];
-                        S->caux[lane] = stage_aux(b.aux4_s[s + lane], c.visc);
+                        S->caux[lane] = stage_aux_t<kPrecise>(b.aux4_s[s + lane], c.visc);
                     }
                     __syncwarp();
                     mask = valid ? chunk_hits<kPrecise>(S->cpos, surv, xi, c.r2) : 0u;
@@ -935,6 +982,7 @@ __global__ void __launch_bounds__(128, 7) k_force(const StepConst cp, const Buff
                 if (!H) continue;
                 list_hits(S->plist, mask, o, lane);
                 __syncwarp();
+                float px = 0.0f, py = 0.0f, pz = 0.0f;  // precision mode: this chunk's sums
                 for (uint32_t base = 0; base < H; base += kForceBatch) {
                     const uint32_t end = min(H, base + kForceBatch);
                     for (uint32_t f = base + lane; f < end; f += 32) {
@@ -952,12 +1000,15 @@ __global__ void __launch_bounds__(128, 7) k_force(const StepConst cp, const Buff
                             S->tbB[u] = Bp;
                             continue;
                         }
-                        if (kPrecise)
-                            force_term_p<kKern>(c, S->tpos[tt], vt, vt.w, S->cpos[jj],
-                                                S->cvel[jj], S->caux[jj], p3, v3);
-                        else
-                            force_term<kKern>(c, S->tpos[tt], vt, vt.w, S->cpos[jj],
-                                              S->cvel[jj], S->caux[jj], p3, v3);
+                        if (kPrecise) {
+                            const float3 fv = force_term_fast<kKern>(c, S->tpos[tt], vt, vt.w,
+                                                                     S->cpos[jj], S->cvel[jj],
+                                                                     S->caux[jj]);
+                            S->tbA[u] = make_float4(fv.x, fv.y, fv.z, 0.0f);
+                            continue;
+                        }
+                        force_term<kKern>(c, S->tpos[tt], vt, vt.w, S->cpos[jj], S->cvel[jj],
+                                          S->caux[jj], p3, v3);
                         S->tbA[u] = make_float4(-p3[0], -p3[1], v3[0], v3[1]);
                         S->tbB[u] = make_float2(-p3[2], v3[2]);
                     }
@@ -966,19 +1017,24 @@ __global__ void __launch_bounds__(128, 7) k_force(const StepConst cp, const Buff
                     for (uint32_t k = max(o, base); k < k1; ++k) {
                         const uint32_t u = k - base;
                         const float4 A = S->tbA[u];
-                        const float2 Bv = S->tbB[u];
                         if (kPrecise) {
-                            Fx.add(A.z + A.x);
-                            Fy.add(A.w + A.y);
-                            Fz.add(Bv.y + Bv.x);
+                            px += A.x;
+                            py += A.y;
+                            pz += A.z;
                             continue;
                         }
+                        const float2 Bv = S->tbB[u];
                         // the records hold -(pressure term): three packed additions
                         fpxy = xadd2(fpxy, pk2(A.x, A.y));
                         fvxy = xadd2(fvxy, pk2(A.z, A.w));
                         fz = xadd2(fz, pk2(Bv.x, Bv.y));
                     }
                     __syncwarp();
+                }
+                if (kPrecise) {  // compensated across chunks
+                    Fx.add(px);
+                    Fy.add(py);
+                    Fz.add(pz);
                 }
             }
         }
