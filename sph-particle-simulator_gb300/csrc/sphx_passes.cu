@@ -618,7 +618,12 @@ __global__ void __launch_bounds__(128, kPrecise ? 9 : 10) k_density(const StepCo
         if (valid) {
             if (kPrecise) rho = rk.value();
             const float P = xmul(c.gas, xsub(rho, c.rest));
-            b.aux4_s[i] = make_float4(rho, P, xmul(2.0f, rho), xdiv(xi.w, rho));
+            // the per-candidate factors of the force pass's pair terms, each formed once here
+            // with the rounding the reference applies per pair: exact mode (rho, P, 2 rho,
+            // (m / rho) mu); precision mode (rho, P, m / (2 rho), (m / rho) mu)
+            const float mr = xdiv(xi.w, rho);
+            b.aux4_s[i] = kPrecise ? make_float4(rho, P, 0.5f * mr, mr * c.visc)
+                                   : make_float4(rho, P, xmul(2.0f, rho), xmul(mr, c.visc));
             my_max = max(my_max, nn);
         }
         __syncwarp();
@@ -634,27 +639,6 @@ __global__ void __launch_bounds__(128, kPrecise ? 9 : 10) k_density(const StepCo
 //  sph_engine.cpp:390-443; integrate_leapfrog, cpp:290-310;
 //  ParticleSystem::apply_boundary_conditions, particle.cpp:122-153)
 // ---------------------------------------------------------------------------------------
-// A candidate's (rho, P, 2 rho, m / rho) as the pair terms read it: the last entry
-// multiplied by the viscosity once here, (m_j / rho_j) * mu being the first product of the
-// reference's viscosity term for every target.
-__device__ __forceinline__ float4 stage_aux(float4 a, float visc) {
-    a.w = xmul(a.w, visc);
-    return a;
-}
-
-// Precision mode: a candidate's factors of the fast pair term, formed once per staged
-// candidate from (rho, P, 2 rho, m / rho): m_j / (2 rho_j), m_j P_j / (2 rho_j) and
-// (m_j / rho_j) mu, so that the pressure factor m_j (P_t + P_j) / (2 rho_j) is one FMA.
-__device__ __forceinline__ float4 stage_aux_fast(float4 a, float visc) {
-    const float half_mr = 0.5f * a.w;
-    return make_float4(half_mr, half_mr * a.y, a.w * visc, 0.0f);
-}
-
-template <bool kPrecise>
-__device__ __forceinline__ float4 stage_aux_t(float4 a, float visc) {
-    return kPrecise ? stage_aux_fast(a, visc) : stage_aux(a, visc);
-}
-
 struct ForceSmem {
     float4 box_lo, box_hi;  // tile box (the fallback walk's culling test)
     int2 seg[kMaxSegments]; // the tile's row segments
@@ -729,7 +713,7 @@ __device__ __forceinline__ void force_term(const StepConst& c, const float4& xt,
         }
         lap = K == SPHX_KERNEL_WENDLAND_C2 ? wendland_lap(c, q) : cubic_lap(c, q);
     }
-    const float sv = aj.w;  // (m_j / rho_j) * mu, formed when the candidate is staged
+    const float sv = aj.w;  // (m_j / rho_j) * mu, formed by the density pass
     v3[0] = xmul(xmul(sv, xsub(vj.x, vt.x)), lap);
     v3[1] = xmul(xmul(sv, xsub(vj.y, vt.y)), lap);
     v3[2] = xmul(xmul(sv, xsub(vj.z, vt.z)), lap);
@@ -797,7 +781,7 @@ __device__ __forceinline__ void force_term_cubic_x2(const StepConst& c, const fl
         pz = xmul(sp, xdiv_fixed(gz, c.h, c.rcp_h, c.fast_div_h));
     }
     const float lap = cubic_lap<kNZ>(c, q);
-    const float sv = aj.w;  // (m_j / rho_j) * mu, formed when the candidate is staged
+    const float sv = aj.w;  // (m_j / rho_j) * mu, formed by the density pass
     const f32x2 vxy = xmul2(xmul2(pk2(sv, sv), xsub2(pk2(vj.x, vj.y), pk2(vt.x, vt.y))),
                             pk2(lap, lap));
     const float vz = xmul(xmul(sv, xsub(vj.z, vt.z)), lap);
@@ -809,8 +793,8 @@ __device__ __forceinline__ void force_term_cubic_x2(const StepConst& c, const fl
 // Precision-mode pair term: the pressure and viscosity contributions of candidate j to the
 // force on particle t, summed into one vector (the mode is judged against FP64, not against
 // the reference's summation order), with contracted FP32 arithmetic, the hardware
-// reciprocal square root and exponential, and the per-candidate factors of
-// stage_aux_fast in aj.  Formulas: equations::compute_pressure_force /
+// reciprocal square root and exponential, and the candidate's factors of the density
+// pass in aj = (rho, P, m / (2 rho), (m / rho) mu).  Formulas: equations::compute_pressure_force /
 // compute_viscosity_force (sph_engine.cpp:390-432) with grad W = g * r_vec and
 // laplacian W = lap of the kernel; the pressure term is skipped for |r| < 1e-6.
 template <int K>
@@ -843,8 +827,8 @@ __device__ __forceinline__ float3 force_term_fast(const StepConst& c, const floa
         }
     }
     if (r < 1e-6f) g = 0.0f;
-    const float cp = -fmaf(Pt, aj.x, aj.y) * g;  // -(m_j (P_t + P_j) / (2 rho_j)) g
-    const float cv = aj.z * lap;                  // (m_j / rho_j) mu lap
+    const float cp = -(aj.z * (Pt + aj.y)) * g;  // -(m_j (P_t + P_j) / (2 rho_j)) g
+    const float cv = aj.w * lap;                  // (m_j / rho_j) mu lap
     return make_float3(fmaf(cp, dx, cv * (vj.x - vt.x)), fmaf(cp, dy, cv * (vj.y - vt.y)),
                        fmaf(cp, dz, cv * (vj.z - vt.z)));
 }
@@ -952,7 +936,7 @@ __global__ void __launch_bounds__(128, kPrecise ? 6 : 7) k_force(const StepConst
                         if (kPrecise) pl = frame_pos(b.cell4_s[s + lane], frame, pl, c.cs);
                         S->cpos[lane] = pl;
                         S->cvel[lane] = b.vel4_s[s + lane];
-                        S->caux[lane] = stage_aux_t<kPrecise>(b.aux4_s[s + lane], c.visc);
+                        S->caux[lane] = b.aux4_s[s + lane];
                     }
                     __syncwarp();
                 } else {
@@ -969,7 +953,7 @@ __global__ void __launch_bounds__(128, kPrecise ? 6 : 7) k_force(const StepConst
                     if (!surv) continue;
                     if (surv & (1u << lane)) {
                         S->cvel[lane] = b.vel4_s[s + lane];
-                        S->caux[lane] = stage_aux_t<kPrecise>(b.aux4_s[s + lane], c.visc);
+                        S->caux[lane] = b.aux4_s[s + lane];
                     }
                     __syncwarp();
                     mask = valid ? chunk_hits<kPrecise>(S->cpos, surv, xi, c.r2) : 0u;
