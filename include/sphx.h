@@ -83,6 +83,9 @@ typedef struct sphx_tuning {
                               dt, parameters or scenes change) */
     int tile_particles;    /* particles of one cell per warp work item (tile), 1..32;
                               0 = default (32) */
+    int bulk_copy;         /* 1 = the force pass stages candidate chunks with cp.async.bulk
+                              copies into double buffers (exact mode); 0 = the lanes' own
+                              loads (default) */
 } sphx_tuning;
 
 /* PerformanceStats (src/sph_engine.h:51-59) plus GPU-side diagnostics. */
@@ -214,7 +217,8 @@ int sphx_get_scene_stats(sphx_ctx* ctx, uint32_t scene, sphx_scene_stats* out);
 
 /* Picks the neighbour passes' launch shape for the loaded workload: times two steps of
  * dt for each candidate -- warps per CTA x resident CTAs per SM, then the tile size
- * (particles per warp work item) at the best of those -- restores the particles, times
+ * (particles per warp work item) and the force pass's staging (lane loads or bulk copies)
+ * at the best of those -- restores the particles, times
  * and scene records after every trial, and keeps the fastest in the context.  Returns
  * the launch choice and its time per step (sphx_get_tuning gives all of it).
  * Synchronises.  No counterpart in the reference (its loops are OpenMP over particles). */

@@ -595,6 +595,7 @@ int sphx_create(sphx_ctx** out, size_t capacity, const sphx_tuning* tuning) {
     if (c->tuning.tile_particles <= 0 || c->tuning.tile_particles > kTile)
         c->tuning.tile_particles = kTile;
     c->b.tile_n = c->tuning.tile_particles;
+    c->tuning.bulk_copy = c->tuning.bulk_copy ? 1 : 0;
     int rc = SPHX_OK;
     auto fail = [&](int code) {
         free_all(c);
@@ -611,6 +612,7 @@ int sphx_create(sphx_ctx** out, size_t capacity, const sphx_tuning* tuning) {
     c->L.num_sms = sms > 0 ? sms : 1;
     c->L.warps_per_block = c->tuning.warps_per_block;
     c->L.blocks_per_sm = c->tuning.blocks_per_sm;
+    c->L.bulk_copy = c->tuning.bulk_copy;
     c->L.stream = c->stream;
     c->capacity = capacity;
     int64_t max_cells = c->tuning.max_grid_cells;
@@ -1003,6 +1005,27 @@ int sphx_autotune(sphx_ctx* c, float dt, int* warps_per_block, int* blocks_per_s
     }
     c->b.tile_n = bt;
     c->tuning.tile_particles = bt;
+    // then the force pass's staging: bulk copies against the lanes' own loads
+    int bbulk = c->L.bulk_copy;
+    if (!rc && c->tuning.mode == SPHX_MODE_EXACT) {
+        c->L.bulk_copy = !bbulk;
+        if (!(rc = reset()) && !(rc = run_phases(c, dt, true)) && !(rc = reset())) {
+            SPHX_CUDA(cudaEventRecord(e0, c->stream));
+            if (!(rc = run_phases(c, dt, true)) && !(rc = reset()) &&
+                !(rc = run_phases(c, dt, true))) {
+                SPHX_CUDA(cudaEventRecord(e1, c->stream));
+                SPHX_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.0f;
+                SPHX_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (ms < best) {
+                    best = ms;
+                    bbulk = c->L.bulk_copy;
+                }
+            }
+        }
+    }
+    c->L.bulk_copy = bbulk;
+    c->tuning.bulk_copy = bbulk;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     c->L.warps_per_block = bw;

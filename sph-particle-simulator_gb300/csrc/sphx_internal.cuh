@@ -362,6 +362,62 @@ __device__ __forceinline__ int cell_coord(float x, float inv_cell) {
     return (int)f;
 }
 
+// ---- bulk copies (cp.async.bulk: the TMA unit's 1-D form) and mbarriers ----------------
+// A warp stages a contiguous range of a cell-sorted array into its shared memory with one
+// bulk copy per array, completed on an mbarrier (one arrival: the issuing lane's
+// arrive.expect_tx with the byte count).  Source and destination 16-byte aligned, size a
+// multiple of 16 bytes: whole float4 elements of cudaMalloc'd arrays.  The threads only
+// read the staged buffers; a buffer is reused once every lane has passed a __syncwarp
+// after its last read.
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t arrivals) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(arrivals)
+                 : "memory");
+}
+// makes mbarrier initialisation visible to the bulk-copy (async) proxy
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// orders this thread's earlier shared-memory accesses before later async-proxy accesses
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile(
+        "{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+            smem_u32(bar)),
+        "r"(bytes)
+        : "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes,
+                                              uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_test_parity(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Waits for the phase `parity` of bar to complete, giving up after kMbarWaitLimit polls
+// (each poll may suspend the thread for a short, hardware-defined time): false = gave up.
+constexpr uint32_t kMbarWaitLimit = 1u << 20;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    for (uint32_t it = 0; it < kMbarWaitLimit; ++it)
+        if (mbar_test_parity(bar, parity)) return true;
+    return false;
+}
+
 // ---- precision mode helpers ----------------------------------------------------------
 
 // Neumaier's compensated summation (Neumaier 1974): sum + running correction.
@@ -392,6 +448,7 @@ struct LaunchCtx {
     int num_sms;
     int warps_per_block;
     int blocks_per_sm;
+    int bulk_copy;  // 1: the force pass stages candidates with bulk copies (exact mode)
 };
 
 int launch_begin_step(const LaunchCtx& L, DevState* ds, int reset_bbox);

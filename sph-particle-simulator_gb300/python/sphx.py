@@ -63,7 +63,7 @@ class SphxParams(C.Structure):
 class SphxTuning(C.Structure):
     _fields_ = [("mode", C.c_int), ("warps_per_block", C.c_int), ("blocks_per_sm", C.c_int),
                 ("max_grid_cells", C.c_int64), ("profile", C.c_int), ("graph", C.c_int),
-                ("tile_particles", C.c_int)]
+                ("tile_particles", C.c_int), ("bulk_copy", C.c_int)]
 
 
 class SphxSceneStats(C.Structure):
@@ -251,11 +251,11 @@ class Context:
 
     def __init__(self, capacity: int, *, mode: int = MODE_EXACT, warps_per_block: int = 0,
                  blocks_per_sm: int = 0, max_grid_cells: int = 0, profile: bool = False,
-                 graph: bool = False, tile_particles: int = 0):
+                 graph: bool = False, tile_particles: int = 0, bulk_copy: bool = False):
         self._lib = lib()
         self._h = C.c_void_p()
         t = SphxTuning(mode, warps_per_block, blocks_per_sm, max_grid_cells, int(profile),
-                       int(graph), tile_particles)
+                       int(graph), tile_particles, int(bulk_copy))
         self._check(self._lib.sphx_create(C.byref(self._h), capacity, C.byref(t)), "sphx_create")
         self.capacity = capacity
 

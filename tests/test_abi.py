@@ -41,7 +41,7 @@ def test_struct_layouts_match_header():
     # 16 floats in SPHParameters order; fixed-width stats record
     assert C.sizeof(sphx.SphxParams) == 64
     assert [f for f, _ in sphx.SphxParams._fields_][-1] == "neighbor_search_radius"
-    assert C.sizeof(sphx.SphxTuning) == 40  # 6 ints + int64, padded
+    assert C.sizeof(sphx.SphxTuning) == 40  # 7 ints + int64
     assert C.sizeof(sphx.SphxStats) == 5 * 8 + 3 * 8 + 2 * 4 + 4 * 4 + 7 * 8 + 8
 
 

@@ -294,3 +294,33 @@ def test_gpu_tile_sizes_keep_every_field_bit_exact(port, tile):
     out, ref = ctx.download(), e.get()
     for k in ("pos", "vel", "rho", "pressure", "acc"):
         assert_bits(out[k], ref[k], k)
+
+
+@pytest.mark.parametrize("case", ["lattice_60k", "crowded", "edge"])
+def test_gpu_bulk_copy_staging_keeps_every_field_bit_exact(port, golden, case):
+    """The force pass's bulk-copy staging (cp.async.bulk into double buffers, a tuning
+    choice) changes only how candidates reach shared memory: one step bit-identical to the
+    oracle on the lattice, a crowded cell and the reference's edge fixture."""
+    if case == "lattice_60k":
+        w = I.scaled_dam_break(60_000, seed=17)
+        pos, vel, mass, prm, dt = w.pos, w.vel, w.mass, w.params, w.dt
+    elif case == "crowded":
+        rng = np.random.default_rng(12)
+        pos = (0.5 + rng.random((640, 3)) * 0.015).astype(np.float32)
+        vel = (rng.standard_normal((640, 3)) * 0.1).astype(np.float32)
+        mass = np.full(640, 1e-3, np.float32)
+        prm, dt = I.params16(xmin=0, xmax=1, ymin=0, ymax=1, zmin=0, zmax=1), 1e-4
+    else:
+        g = golden_case(golden, "edge")
+        pos, vel, mass, prm, dt = g["pos"], g["vel"], g["mass"], g["params"], 1e-3
+    n = pos.shape[0]
+    ctx = make_ctx(n, prm, pos, vel, mass, bulk_copy=True)
+    assert ctx.tuning()["bulk_copy"] == 1
+    ctx.step(dt)
+    e = O.Engine(port, n)
+    e.initialize(prm)
+    e.add(pos, vel, mass)
+    e.step(dt)
+    out, ref = ctx.download(), e.get()
+    for k in ("pos", "vel", "rho", "pressure", "acc"):
+        assert_bits(out[k], ref[k], k)
