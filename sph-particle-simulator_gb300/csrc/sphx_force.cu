@@ -253,10 +253,19 @@ __device__ __forceinline__ void integrate_cells(const StepConst& c, float dt, co
     }
 }
 
-template <bool kIntegrate, bool kPrecise, bool kBatch, int kKern, bool kNZ, bool kBulk>
-__global__ void __launch_bounds__(128, kPrecise || kBulk ? 6 : 7) k_force(const StepConst cp, const Buffers b,
-                                               DevState* ds) {
+// Cells holding more particles than this after the grid build mark a collapsed state, in
+// which whole chunks are dense (every particle of a tile within r of every candidate).
+constexpr uint32_t kDenseOccupancy = 128;
+
+// kDense: the variant with the dense-chunk path (lane-load staging only).  With lane-load
+// staging both variants are launched every step and each returns at once unless the grid's
+// fullest cell says the state is its case.
+template <bool kIntegrate, bool kPrecise, bool kBatch, int kKern, bool kNZ, bool kBulk,
+          bool kDense>
+__global__ void __launch_bounds__(128, kPrecise || kBulk || kDense ? 6 : 7) k_force(
+    const StepConst cp, const Buffers b, DevState* ds) {
     if (ds->status) return;
+    if (!kBulk && kDense != (ds->max_occ > kDenseOccupancy)) return;
     extern __shared__ __align__(16) unsigned char smem_raw_f[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     ForceSmem<kBulk>* S = reinterpret_cast<ForceSmem<kBulk>*>(smem_raw_f) + warp;
@@ -305,7 +314,7 @@ __global__ void __launch_bounds__(128, kPrecise || kBulk ? 6 : 7) k_force(const 
         // One chunk's work once its candidates are staged (cpos/cvel/caux) and this lane's
         // hit mask is known: list the warp's hits, compute the pair terms flattened, and
         // add every lane's own terms in candidate order.
-        auto process = [&](uint32_t mask, int s, const float4* cpos, const float4* cvel,
+        auto process = [&](uint32_t mask, int s, int m, const float4* cpos, const float4* cvel,
                            const float4* caux) {
             const int self = i - s;
             if ((unsigned)self < 32u) mask &= ~(1u << self);
@@ -313,6 +322,58 @@ __global__ void __launch_bounds__(128, kPrecise || kBulk ? 6 : 7) k_force(const 
             uint32_t H;
             const uint32_t o = warp_excl_scan(cnt, lane, H);
             if (!H) return;
+            // dense chunk (collapsed cells): the warp's hits are every (particle, candidate)
+            // pair of the chunk except the self pairs.  Each lane then forms its own terms,
+            // candidate after candidate, and adds them to its sums: the flattened path's
+            // terms (same inputs from shared memory) and additions, in the same order.  The
+            // additions are scalar IEEE adds on the unpacked sums: the packed FP32x2 add fed
+            // directly with the term values in registers gave last-bit differences in some
+            // collapsed states (measured against the reference's fixtures), while scalar adds
+            // (or a round trip of the terms through shared memory, as the flattened fold
+            // does) are exact.
+            const int lo = max(T.k0, s), hi = min(T.k0 + T.cnt, s + m);
+            if (kDense && H == (uint32_t)(T.cnt * m - max(hi - lo, 0))) {
+                const float4 xt = S->tpos[lane], vt = S->tvel[lane];
+                float px = 0.0f, py = 0.0f, pz = 0.0f;
+                float2 sp = upk2(fpxy), sv = upk2(fvxy), sz = upk2(fz);
+                for (int jj = 0; jj < m; ++jj) {
+                    if (!valid || jj == self) continue;
+                    if (kPrecise) {
+                        const float3 fv =
+                            force_term_fast<kKern>(c, xt, vt, vt.w, cpos[jj], cvel[jj], caux[jj]);
+                        px += fv.x;
+                        py += fv.y;
+                        pz += fv.z;
+                        continue;
+                    }
+                    float4 A;
+                    float2 Bv;
+                    if (kKern == SPHX_KERNEL_CUBIC_SPLINE) {
+                        force_term_cubic_x2<kNZ>(c, xt, vt, vt.w, cpos[jj], cvel[jj], caux[jj], A,
+                                                 Bv);
+                    } else {
+                        float p3[3], v3[3];
+                        force_term<kKern>(c, xt, vt, vt.w, cpos[jj], cvel[jj], caux[jj], p3, v3);
+                        A = make_float4(-p3[0], -p3[1], v3[0], v3[1]);
+                        Bv = make_float2(-p3[2], v3[2]);
+                    }
+                    sp.x = xadd(sp.x, A.x);
+                    sp.y = xadd(sp.y, A.y);
+                    sv.x = xadd(sv.x, A.z);
+                    sv.y = xadd(sv.y, A.w);
+                    sz.x = xadd(sz.x, Bv.x);
+                    sz.y = xadd(sz.y, Bv.y);
+                }
+                fpxy = pk2(sp.x, sp.y);
+                fvxy = pk2(sv.x, sv.y);
+                fz = pk2(sz.x, sz.y);
+                if (kPrecise) {
+                    Fx.add(px);
+                    Fy.add(py);
+                    Fz.add(pz);
+                }
+                return;
+            }
             list_hits(S->plist, mask, o, lane);
             __syncwarp();
             float px = 0.0f, py = 0.0f, pz = 0.0f;  // precision mode: this chunk's sums
@@ -419,7 +480,7 @@ __global__ void __launch_bounds__(128, kPrecise || kBulk ? 6 : 7) k_force(const 
                         __syncwarp();
                         mask = valid ? chunk_hits<kPrecise>(S->cpos[0], surv, xi, c.r2) : 0u;
                     }
-                    process(mask, s, S->cpos[0], S->cvel[0], S->caux[0]);
+                    process(mask, s, m, S->cpos[0], S->cvel[0], S->caux[0]);
                 }
             }
         } else {
@@ -485,7 +546,7 @@ __global__ void __launch_bounds__(128, kPrecise || kBulk ? 6 : 7) k_force(const 
                             __ballot_sync(kFull, lane < m && box_near(B, cpos[lane], r2m));
                         mask = valid && surv ? chunk_hits<false>(cpos, surv, xi, c.r2) : 0u;
                     }
-                    process(mask, s, cpos, S->cvel[q], S->caux[q]);
+                    process(mask, s, m, cpos, S->cvel[q], S->caux[q]);
                     __syncwarp();  // buffer q is free once every lane is past this point
                     if (next_staged) q ^= 1;
                     cur_staged = next_staged;
@@ -567,61 +628,64 @@ __global__ void __launch_bounds__(128, kPrecise || kBulk ? 6 : 7) k_force(const 
     }
 }
 
-template <bool kIntegrate, bool kPrecise, bool kBatch, int kKern, bool kNZ, bool kBulk>
+template <bool kIntegrate, bool kPrecise, bool kBatch, int kKern, bool kNZ, bool kBulk,
+          bool kDense>
 static void launch_force_v(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                            DevState* ds) {
     const int threads = 32 * L.warps_per_block;
     const size_t sm = (size_t)L.warps_per_block * sizeof(ForceSmem<kBulk>);
     static LaunchShapeCache cache;
     const int nb = cached_resident_blocks(
-        cache, L, k_force<kIntegrate, kPrecise, kBatch, kKern, kNZ, kBulk>, threads, sm);
-    k_force<kIntegrate, kPrecise, kBatch, kKern, kNZ, kBulk><<<nb, threads, sm, L.stream>>>(c, b, ds);
+        cache, L, k_force<kIntegrate, kPrecise, kBatch, kKern, kNZ, kBulk, kDense>, threads, sm);
+    k_force<kIntegrate, kPrecise, kBatch, kKern, kNZ, kBulk, kDense>
+        <<<nb, threads, sm, L.stream>>>(c, b, ds);
 }
 
 // Exact mode stages candidates by the lanes' own loads or by bulk copies (L.bulk_copy, a
 // tuning choice); precision mode by the lanes' loads (its candidates are converted to the
-// tile's frame as they are staged).
+// tile's frame as they are staged).  Returns the kernels launched.
 template <bool kIntegrate, bool kPrecise, bool kBatch, int kKern, bool kNZ = false>
-static void launch_force_t(const LaunchCtx& L, const StepConst& c, const Buffers& b,
-                           DevState* ds) {
+static int launch_force_t(const LaunchCtx& L, const StepConst& c, const Buffers& b,
+                          DevState* ds) {
     if constexpr (!kPrecise) {
         if (L.bulk_copy) {
-            launch_force_v<kIntegrate, kPrecise, kBatch, kKern, kNZ, true>(L, c, b, ds);
-            return;
+            launch_force_v<kIntegrate, kPrecise, kBatch, kKern, kNZ, true, false>(L, c, b, ds);
+            return 1;
         }
     }
-    launch_force_v<kIntegrate, kPrecise, kBatch, kKern, kNZ, false>(L, c, b, ds);
+    launch_force_v<kIntegrate, kPrecise, kBatch, kKern, kNZ, false, false>(L, c, b, ds);
+    launch_force_v<kIntegrate, kPrecise, kBatch, kKern, kNZ, false, true>(L, c, b, ds);
+    return 2;
 }
 
 template <int kKern>
-static void launch_force_k(const LaunchCtx& L, const StepConst& c, const Buffers& b,
-                           DevState* ds, int integrate) {
+static int launch_force_k(const LaunchCtx& L, const StepConst& c, const Buffers& b,
+                          DevState* ds, int integrate) {
     const bool nz = kKern == SPHX_KERNEL_CUBIC_SPLINE && !c.precise && c.div_nz;
     if (b.nscenes > 0) {
         if (integrate) {
-            if (nz) launch_force_t<true, false, true, kKern, true>(L, c, b, ds);
-            else launch_force_t<true, false, true, kKern>(L, c, b, ds);
-        } else launch_force_t<false, false, true, kKern>(L, c, b, ds);
-    } else if (integrate) {
-        if (c.precise) launch_force_t<true, true, false, kKern>(L, c, b, ds);
-        else if (nz) launch_force_t<true, false, false, kKern, true>(L, c, b, ds);
-        else launch_force_t<true, false, false, kKern>(L, c, b, ds);
-    } else {
-        if (c.precise) launch_force_t<false, true, false, kKern>(L, c, b, ds);
-        else if (nz) launch_force_t<false, false, false, kKern, true>(L, c, b, ds);
-        else launch_force_t<false, false, false, kKern>(L, c, b, ds);
+            if (nz) return launch_force_t<true, false, true, kKern, true>(L, c, b, ds);
+            return launch_force_t<true, false, true, kKern>(L, c, b, ds);
+        }
+        return launch_force_t<false, false, true, kKern>(L, c, b, ds);
     }
+    if (integrate) {
+        if (c.precise) return launch_force_t<true, true, false, kKern>(L, c, b, ds);
+        if (nz) return launch_force_t<true, false, false, kKern, true>(L, c, b, ds);
+        return launch_force_t<true, false, false, kKern>(L, c, b, ds);
+    }
+    if (c.precise) return launch_force_t<false, true, false, kKern>(L, c, b, ds);
+    if (nz) return launch_force_t<false, false, false, kKern, true>(L, c, b, ds);
+    return launch_force_t<false, false, false, kKern>(L, c, b, ds);
 }
 
 int launch_force(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds,
                  int integrate) {
     if (c.kern == SPHX_KERNEL_WENDLAND_C2)
-        launch_force_k<SPHX_KERNEL_WENDLAND_C2>(L, c, b, ds, integrate);
-    else if (c.kern == SPHX_KERNEL_GAUSSIAN)
-        launch_force_k<SPHX_KERNEL_GAUSSIAN>(L, c, b, ds, integrate);
-    else
-        launch_force_k<SPHX_KERNEL_CUBIC_SPLINE>(L, c, b, ds, integrate);
-    return 1;
+        return launch_force_k<SPHX_KERNEL_WENDLAND_C2>(L, c, b, ds, integrate);
+    if (c.kern == SPHX_KERNEL_GAUSSIAN)
+        return launch_force_k<SPHX_KERNEL_GAUSSIAN>(L, c, b, ds, integrate);
+    return launch_force_k<SPHX_KERNEL_CUBIC_SPLINE>(L, c, b, ds, integrate);
 }
 
 }  // namespace sphx
