@@ -220,13 +220,13 @@ def run_cpu(w: I.Workload, steps: int, warmup: int, budget_s: float | None = Non
             "sample": f"{w.name}: {w.n} particles, {len(times)} fresh-state steps"}
 
 
-def workload_config(w: I.Workload, workload_name: str, world: int) -> dict:
+def workload_config(w: I.Workload, workload_name: str, world: int, mode: str = "exact") -> dict:
     """The `config` object of both arms' JSON lines: the workload and its protocol."""
     return {
         "workload": workload_name, "particles": w.n,
         "lattice": "x".join(map(str, w.info.get("lattice", ()))), "dt": w.dt,
         "protocol": "fresh-state (initial state restored before each step)",
-        "l2": "GPU arm: flushed between timed steps (512 MiB write)", "mode": "exact",
+        "l2": "GPU arm: flushed between timed steps (512 MiB write)", "mode": mode,
         "parallelism": f"replicas x{world}",
     }
 
@@ -569,7 +569,8 @@ def bench_ours(args, world, rank, local):
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
     # per-phase kernel times: an eager, profiled context (events around each phase)
-    prof = sphx.Context(w.n, profile=True)
+    mode = sphx.MODE_PRECISE if args.mode == "precise" else sphx.MODE_EXACT
+    prof = sphx.Context(w.n, profile=True, mode=mode)
     prof.set_stream(stream.cuda_stream)
     prof.set_params(w.params)
     prof.upload(w.pos, w.vel, w.mass)
@@ -587,7 +588,7 @@ def bench_ours(args, world, rank, local):
     grid_s = pst["neighbor_search_time"] / args.steps
 
     # the measured path: the step captured once as a CUDA graph and replayed
-    ctx = sphx.Context(w.n, graph=True)
+    ctx = sphx.Context(w.n, graph=True, mode=mode)
     ctx.set_stream(stream.cuda_stream)
     ctx.set_params(w.params)
     ctx.upload(w.pos, w.vel, w.mass)
@@ -731,7 +732,7 @@ def bench_ours(args, world, rank, local):
         "higher_is_better": True, "scaling": "weak",
         "vs_baseline": value / PUBLISHED_1M if args.workload == "dam_break_1M" else None,
         "dtype": "f32", "data": "synthetic",
-        "config": workload_config(w, args.workload, world),
+        "config": workload_config(w, args.workload, world, args.mode),
         "launch": "step captured as a CUDA graph and replayed (sphx_tuning.graph); "
                   "eager launches: %.4f ms/step" % (sum(ms_eager) / args.steps),
         "vs_baseline_ref": "README.md:45 CPU 1M 38 steps/s = 3.8e7 particle-steps/s",
@@ -778,6 +779,9 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-scene figure")
     ap.add_argument("--no-faithful", action="store_true",
                     help="skip the faithful-trajectory figure")
+    ap.add_argument("--mode", choices=("exact", "precise"), default="exact",
+                    help="the main workload's mode (precise: cell + offset storage, fast "
+                         "pair arithmetic, compensated sums)")
     ap.add_argument("--no-dropin", action="store_true",
                     help="skip the drop-in engine's end-to-end figure")
     args = ap.parse_args()
