@@ -212,7 +212,7 @@ int launch_batch_grid(const LaunchCtx& L, const Buffers& b, DevState* ds, int n,
     k_batch_bbox<<<gb, 256, 0, L.stream>>>(b.pos4, b.scene_of, n, b.scenes);
     k_batch_grid_setup<<<1, 32, 0, L.stream>>>(b.scenes, b.nscenes, max_cells, ds);
     k_batch_keys<<<gb, 256, 0, L.stream>>>(b.pos4, b.scene_of, n, b.scenes, ds, b.key[0]);
-    return 3 + launch_grid_sort(L, b, ds, n);
+    return 3 + launch_grid_sort(L, b, ds, n, 0.0f);
 }
 
 // ---- FP64 diagnostics per scene (one block per scene, fixed order) ----------------------

@@ -595,6 +595,7 @@ int sphx_create(sphx_ctx** out, size_t capacity, const sphx_tuning* tuning) {
     if (c->tuning.tile_particles <= 0 || c->tuning.tile_particles > kTile)
         c->tuning.tile_particles = kTile;
     c->b.tile_n = c->tuning.tile_particles;
+    c->b.columns = c->tuning.mode != SPHX_MODE_EXACT ? 1 : 0;  // the precision-mode sweeps' tiles
     c->tuning.bulk_copy = c->tuning.bulk_copy ? 1 : 0;
     int rc = SPHX_OK;
     auto fail = [&](int code) {
@@ -1302,10 +1303,13 @@ int sphx_debug_pairs(sphx_ctx* c, int64_t* counts, int64_t* idx, size_t* total_i
     fill_step_const(c);
     c->have_fields = false;  // the grid rebuild below replaces the sorted permutation
     launch_begin_step(c->L, c->ds, 1);
-    launch_build_grid(c->L, c->sc, c->b, c->ds);
+    // the lists come in the reference's order: insertion order within each cell
+    Buffers bq = c->b;
+    bq.columns = 0;
+    launch_build_grid(c->L, c->sc, bq, c->ds);
     uint32_t* d_cnt = nullptr;
     if ((rc = dmalloc(&d_cnt, n))) return rc;
-    launch_pair_counts(c->L, c->sc, c->b, c->ds, d_cnt);
+    launch_pair_counts(c->L, c->sc, bq, c->ds, d_cnt);
     std::vector<uint32_t> h_cnt(n);
     cudaError_t e = cudaMemcpyAsync(h_cnt.data(), d_cnt, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
@@ -1333,7 +1337,7 @@ int sphx_debug_pairs(sphx_ctx* c, int64_t* counts, int64_t* idx, size_t* total_i
     }
     e = cudaMemcpyAsync(d_off, off.data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) {
-        launch_pair_fill(c->L, c->sc, c->b, c->ds, d_off, d_out);
+        launch_pair_fill(c->L, c->sc, bq, c->ds, d_off, d_out);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess)
@@ -1361,10 +1365,13 @@ int sphx_debug_pairs_subset(sphx_ctx* c, size_t nsel, const int64_t* sel, int64_
     fill_step_const(c);
     c->have_fields = false;  // the grid rebuild below replaces the sorted permutation
     launch_begin_step(c->L, c->ds, 1);
-    launch_build_grid(c->L, c->sc, c->b, c->ds);
+    // the lists come in the reference's order: insertion order within each cell
+    Buffers bq = c->b;
+    bq.columns = 0;
+    launch_build_grid(c->L, c->sc, bq, c->ds);
     uint32_t* d_cnt = nullptr;
     if ((rc = dmalloc(&d_cnt, n))) return rc;
-    launch_pair_counts(c->L, c->sc, c->b, c->ds, d_cnt);
+    launch_pair_counts(c->L, c->sc, bq, c->ds, d_cnt);
     std::vector<uint32_t> h_cnt(n);
     cudaError_t e = cudaMemcpyAsync(h_cnt.data(), d_cnt, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
@@ -1398,7 +1405,7 @@ int sphx_debug_pairs_subset(sphx_ctx* c, size_t nsel, const int64_t* sel, int64_
     std::vector<int64_t> lists(uniq_total ? uniq_total : 1);
     e = cudaMemcpyAsync(d_off, off.data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) {
-        launch_pair_fill(c->L, c->sc, c->b, c->ds, d_off, d_out);
+        launch_pair_fill(c->L, c->sc, bq, c->ds, d_off, d_out);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess && uniq_total)

@@ -217,7 +217,7 @@ static void launch_density_k(const LaunchCtx& L, const StepConst& c, const Buffe
     if (b.nscenes > 0) {
         if (nz) launch_density_t<false, true, kKern, true>(L, c, b, ds);
         else launch_density_t<false, true, kKern>(L, c, b, ds);
-    } else if (c.precise) launch_density_t<true, false, kKern>(L, c, b, ds);
+    } else if (c.precise) launch_density_sweep(L, c, b, ds);
     else if (nz) launch_density_t<false, false, kKern, true>(L, c, b, ds);
     else launch_density_t<false, false, kKern>(L, c, b, ds);
 }

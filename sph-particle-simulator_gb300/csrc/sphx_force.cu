@@ -213,46 +213,6 @@ __device__ __forceinline__ float3 force_term_fast(const StepConst& c, const floa
                        fmaf(cp, dz, cv * (vj.z - vt.z)));
 }
 
-// Precision-mode leapfrog + wall clamp on cell + offset positions (FP64 clamp).
-__device__ __forceinline__ void integrate_cells(const StepConst& c, float dt, const float* acc,
-                                                float* o, float* v, int4& cell) {
-    int* cc[3] = {&cell.x, &cell.y, &cell.z};
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const float half = 0.5f * acc[a] * dt;
-        float vv = v[a] + half;
-        float on = o[a] + vv * dt;
-        vv = vv + half;
-        v[a] = vv * c.damping;
-        if (!isfinite(on)) {  // the position is lost: park the particle as non-finite
-            cell.w = 1;
-            o[a] = on;
-            continue;
-        }
-        double X = (double)(*cc[a]) * c.cs_d + (double)on;
-        if (X < (double)c.lo[a]) {
-            X = c.lo[a];
-            v[a] = v[a] * -0.8f;
-        } else if (X > (double)c.hi[a]) {
-            X = c.hi[a];
-            v[a] = v[a] * -0.8f;
-        }
-        double f = floor(X / c.cs_d);
-        f = fmin(fmax(f, -(double)kCellClamp), (double)(kCellClamp - 1));
-        int ci = (int)f;
-        float oo = (float)(X - (double)ci * c.cs_d);
-        if (c.fp16) oo = round_half(oo);
-        if (oo >= c.cs) {
-            oo = 0.0f;
-            ci += 1;
-        } else if (oo < 0.0f) {
-            oo = 0.0f;
-        }
-        *cc[a] = ci;
-        o[a] = oo;
-    }
-}
-
 // Cells holding more particles than this after the grid build mark a collapsed state, in
 // which whole chunks are dense (every particle of a tile within r of every candidate).
 constexpr uint32_t kDenseOccupancy = 128;
@@ -670,11 +630,11 @@ static int launch_force_k(const LaunchCtx& L, const StepConst& c, const Buffers&
         return launch_force_t<false, false, true, kKern>(L, c, b, ds);
     }
     if (integrate) {
-        if (c.precise) return launch_force_t<true, true, false, kKern>(L, c, b, ds);
+        if (c.precise) return launch_force_sweep(L, c, b, ds, 1);
         if (nz) return launch_force_t<true, false, false, kKern, true>(L, c, b, ds);
         return launch_force_t<true, false, false, kKern>(L, c, b, ds);
     }
-    if (c.precise) return launch_force_t<false, true, false, kKern>(L, c, b, ds);
+    if (c.precise) return launch_force_sweep(L, c, b, ds, 0);
     if (nz) return launch_force_t<false, false, false, kKern, true>(L, c, b, ds);
     return launch_force_t<false, false, false, kKern>(L, c, b, ds);
 }

@@ -309,6 +309,68 @@ __global__ void k_offsets(const uint32_t* __restrict__ key_s, int n, const DevSt
     }
 }
 
+// Precision-mode step (b.columns): each cell's particles put in z order (the in-cell
+// offset quantised to 16 levels of cs/16, stable within a level), so that a run of
+// consecutive particles of a cell column -- a tile -- is a compact slab across the cells.
+// The order within a cell is free in this mode (its sums are judged against FP64, not
+// against the reference's order).  One warp per cell; cells of more than kZOrderMax
+// particles (collapsed states, whose tiles are dense anyway) keep their order.
+constexpr int kZOrderMax = 128;
+__global__ void __launch_bounds__(256) k_cell_zorder(const Buffers b, const DevState* ds,
+                                                     float levels_per_unit) {
+    if (ds->status) return;
+    constexpr int kPer = kZOrderMax / 32;
+    const uint32_t nc = ds->ncells;
+    const int lane = threadIdx.x & 31;
+    const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+    const uint32_t lt = (1u << lane) - 1u;
+    for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < nc; c += nwarps) {
+        const uint32_t a = b.off[c], cnt = b.off[c + 1] - a;
+        if (cnt < 2 || cnt > (uint32_t)kZOrderMax) continue;
+        float4 p[kPer], v[kPer];
+        int4 ce[kPer];
+        uint32_t id[kPer];
+        int lev[kPer];
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const uint32_t q = (uint32_t)(j * 32 + lane);
+            lev[j] = 16;  // no element
+            if (q < cnt) {
+                p[j] = b.pos4_s[a + q];
+                v[j] = b.vel4_s[a + q];
+                ce[j] = b.cell4_s[a + q];
+                id[j] = b.id_s[a + q];
+                lev[j] = min(15, max(0, (int)(p[j].z * levels_per_unit)));
+            }
+        }
+        // stable counting sort over the 16 levels: an element's place is the number of
+        // elements of lower levels plus those of its level before it
+        int dest[kPer];
+        uint32_t below = 0;
+#pragma unroll 1
+        for (int L = 0; L < 16; ++L) {
+            uint32_t seen = below;
+#pragma unroll
+            for (int j = 0; j < kPer; ++j) {
+                const uint32_t m = __ballot_sync(0xffffffffu, lev[j] == L);
+                if (lev[j] == L) dest[j] = (int)(seen + __popc(m & lt));
+                seen += __popc(m);
+            }
+            below = seen;
+        }
+        __syncwarp();  // every lane holds its elements: the cell's range can be rewritten
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            if (lev[j] == 16) continue;
+            const uint32_t k = a + (uint32_t)dest[j];
+            b.pos4_s[k] = p[j];
+            b.vel4_s[k] = v[j];
+            b.cell4_s[k] = ce[j];
+            b.id_s[k] = id[j];
+        }
+    }
+}
+
 int launch_build_grid(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                       DevState* ds) {
     const int n = c.n;
@@ -318,17 +380,27 @@ int launch_build_grid(const LaunchCtx& L, const StepConst& c, const Buffers& b,
     k_grid_setup<<<1, 32, 0, L.stream>>>(n, c.max_cells, ds);
     if (c.precise) k_keys_cells<<<gb, 256, 0, L.stream>>>(b.cell4, n, ds, b.key[0]);
     else k_keys<<<gb, 256, 0, L.stream>>>(b.pos4, n, c.inv_cell, ds, b.key[0]);
-    return 3 + launch_grid_sort(L, b, ds, n);
+    return 3 + launch_grid_sort(L, b, ds, n, c.cs);
+}
+
+static int launch_cell_zorder(const LaunchCtx& L, const Buffers& b, DevState* ds, int n,
+                              float cs) {
+    if (!b.columns || !b.cell4_s) return 0;
+    // one warp per cell: blocks of 8 warps, enough of them for the occupied cells
+    k_cell_zorder<<<grid_blocks(L, n, 256, 8), 256, 0, L.stream>>>(b, ds, 16.0f / cs);
+    return 1;
 }
 
 // Shared tail of the grid build: stable sort of the keys, gather into cell-sorted order,
-// cell offsets, tile list.
-int launch_grid_sort(const LaunchCtx& L, const Buffers& b, DevState* ds, int n) {
+// cell offsets, (b.columns) z order within the cells, tile list.
+int launch_grid_sort(const LaunchCtx& L, const Buffers& b, DevState* ds, int n, float cs) {
     const int r = launch_radix_sort(L, b, ds, n);
     k_reorder<<<grid_blocks(L, n, 256, 8), 256, 0, L.stream>>>(b, n, ds);
     k_offsets<<<grid_blocks(L, n + 1, 256, 8), 256, 0, L.stream>>>(b.key_s, n, ds, b.off);
-    return 2 + r + launch_tile_scan(L, b, ds, n);
+    const int z = launch_cell_zorder(L, b, ds, n, cs);
+    return 2 + r + z + launch_tile_scan(L, b, ds, n);
 }
+
 
 // ---- FP64 diagnostics of the state after a step -----------------------------------------
 // sums: mass, momentum x/y/z, kinetic energy, potential energy (-m g y), density.

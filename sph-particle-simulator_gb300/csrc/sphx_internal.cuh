@@ -136,6 +136,10 @@ struct Buffers {
     int scan_part_cap;
     int diag_blocks;
     int tile_n = kTile;  // particles per warp work item (1 .. kTile)
+    // 1 (precision-mode step): each cell's particles are put in z order after the sort and
+    // the tiles run along cell columns (x, y, *), spanning cells; 0: the reference's
+    // insertion order within each cell and tiles within one cell
+    int columns = 0;
 };
 constexpr uint32_t kNoSlot = 0xffffffffu;
 constexpr uint64_t kNoPairs = ~0ull;  // pair fill: this particle's list is not wanted
@@ -456,11 +460,17 @@ int launch_cfl(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevStat
                 float host_dt);
 int launch_build_grid(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                        DevState* ds);
-int launch_grid_sort(const LaunchCtx& L, const Buffers& b, DevState* ds, int n);
+// cs: the precision mode's cell size (the in-cell z order of b.columns; else unused)
+int launch_grid_sort(const LaunchCtx& L, const Buffers& b, DevState* ds, int n, float cs);
 int launch_density(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds);
 int launch_force(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds,
                   int integrate);
 int launch_diag(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds);
+// precision mode (single scene): the tile-sweep passes (sphx_sweep.cu)
+int launch_density_sweep(const LaunchCtx& L, const StepConst& c, const Buffers& b,
+                         DevState* ds);
+int launch_force_sweep(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds,
+                       int integrate);
 void launch_pair_counts(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                         DevState* ds, uint32_t* counts_by_id);
 void launch_pair_fill(const LaunchCtx& L, const StepConst& c, const Buffers& b,

@@ -3,11 +3,12 @@
 // the stencil walk, the chunk machinery, the pair arithmetic helpers and the launch-shape
 // cache.
 //
-// Work decomposition: one warp owns one tile (up to 32 consecutive cell-sorted particles
-// of one cell, one particle per lane).  All lanes of a tile share the tile's stencil:
-// for each row (dx, dy) the cells cz+lo..cz+hi are one contiguous range of the sorted
-// arrays; the warp stages that range through shared memory 32 candidates at a time and
-// every lane tests every candidate against its own particle.
+// Work decomposition: one warp owns one tile (up to 32 consecutive cell-sorted particles of
+// one cell column (x, y, *), one particle per lane; a tile may span several cells of its
+// column).  All lanes of a tile share the tile's stencil: for each row (dx, dy) the cells
+// cz+lo..cz+hi (covering every lane's cell +-1, +-2 near a face) are one contiguous range
+// of the sorted arrays; the warp stages that range through shared memory 32 candidates at
+// a time and every lane tests every candidate against its own particle.
 //
 // Exactness.  The reference walks, for particle i, the cells (dx, dy, dz) of its stencil
 // in lexicographic order and each cell's particles in insertion order
@@ -17,8 +18,11 @@
 // each row in increasing z, so a lane meets its neighbours in exactly the reference's
 // order.  The reference scans a 5x5x5 block (cell_radius = 2); a neighbour at distance
 // <= r can only sit two cells away when the particle lies within rounding distance of a
-// cell face, so the tile's stencil is 3x3x3, widened on an axis to the second layer when
-// some lane is that close to a face (guard band eps below).  Every distance test and
+// cell face, so the tile's stencil is the 3x3x3 block of each of its cells, widened on an
+// axis to the second layer when some lane is that close to a face (guard band eps below).
+// Cells of the tile's rows outside a lane's own 5x5x5 block hold no neighbour of it (they
+// are more than two cells away), so they add only misses to that lane's walk, and the
+// cells of its block keep their relative order.  Every distance test and
 // every term uses the reference's float operations in the reference's order with
 // IEEE round-to-nearest and no contraction, so each lane's sums are bit-identical.
 #pragma once
@@ -60,13 +64,32 @@ __device__ __forceinline__ Geom scene_geom(const SceneInfo& sc, const DevState* 
     return g;
 }
 
+// End (sorted position) of the run a tile of cell `key` may fill: the cell, or (b.columns)
+// its cell column (the non-finite group is its own column).
+__device__ __forceinline__ uint32_t tile_run_end(const Buffers& b, const Geom& g, uint32_t key) {
+    if (!b.columns || key >= g.sentinel) return b.off[key + 1];
+    const uint32_t d2 = (uint32_t)g.dim[2];
+    return b.off[g.base + ((key - g.base) / d2 + 1u) * d2];
+}
+
+// The tile's z range relative to its first particle's cell: every lane's cell +-1, or +-2
+// on the side where the lane lies within the guard band of a cell face.
+__device__ __forceinline__ void tile_z_range(const Buffers& b, const Geom& g, uint32_t k0,
+                                             int lane, bool valid, bool near_lo, bool near_hi,
+                                             Tile& T) {
+    const uint32_t kl = valid ? b.key_s[k0 + lane] : b.key_s[k0];
+    const int rz = (int)((kl - g.base) % (uint32_t)g.dim[2]) - T.cz;  // >= 0 (sorted)
+    T.lo[2] = __reduce_min_sync(0xffffffffu, rz + (near_lo ? -2 : -1));
+    T.hi[2] = __reduce_max_sync(0xffffffffu, rz + (near_hi ? 2 : 1));
+}
+
 // Sets up the tile starting at sorted position k0; returns the lane's particle (valid
 // lanes only).
 __device__ __forceinline__ void tile_setup(const StepConst& c, const Buffers& b, const Geom& g,
                                            uint32_t k0, int lane, Tile& T, float4& xi,
                                            bool& valid) {
     const uint32_t key = b.key_s[k0];
-    const uint32_t end = b.off[key + 1];
+    const uint32_t end = tile_run_end(b, g, key);
     T.k0 = (int)k0;
     T.cnt = (int)min(end - k0, (uint32_t)b.tile_n);
     valid = lane < T.cnt;
@@ -79,6 +102,7 @@ __device__ __forceinline__ void tile_setup(const StepConst& c, const Buffers& b,
     T.cy = (int)((local / dz) % dy);
     T.cx = (int)(local / (dz * dy));
     const float x[3] = {xi.x, xi.y, xi.z};
+    bool lo_z = false, hi_z = false;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         // position inside the cell in cell units; the guard band covers the rounding of
@@ -88,9 +112,15 @@ __device__ __forceinline__ void tile_setup(const StepConst& c, const Buffers& b,
         const float eps = 1.52587890625e-5f + fabsf(u) * 9.5367431640625e-7f;
         const bool near_lo = valid && frac < eps;
         const bool near_hi = valid && (1.0f - frac) < eps;
-        T.lo[a] = __any_sync(0xffffffffu, near_lo) ? -2 : -1;
-        T.hi[a] = __any_sync(0xffffffffu, near_hi) ? 2 : 1;
+        if (a == 2) {
+            lo_z = near_lo;
+            hi_z = near_hi;
+        } else {
+            T.lo[a] = __any_sync(0xffffffffu, near_lo) ? -2 : -1;
+            T.hi[a] = __any_sync(0xffffffffu, near_hi) ? 2 : 1;
+        }
     }
+    tile_z_range(b, g, k0, lane, valid, lo_z, hi_z, T);
 }
 
 // Precision mode: the tile's frame is the cell of its first particle; a position inside
@@ -108,7 +138,7 @@ __device__ __forceinline__ void tile_setup_cells(const StepConst& c, const Buffe
                                                  int4& frame) {
     const uint32_t key = b.key_s[k0];
     const uint32_t nc = g.sentinel;
-    const uint32_t end = b.off[key + 1];
+    const uint32_t end = tile_run_end(b, g, key);
     T.k0 = (int)k0;
     T.cnt = (int)min(end - k0, (uint32_t)b.tile_n);
     valid = lane < T.cnt;
@@ -128,13 +158,20 @@ __device__ __forceinline__ void tile_setup_cells(const StepConst& c, const Buffe
     T.cx = (int)(local / (dz * dy));
     const float off[3] = {o.x, o.y, o.z};
     const float eps = c.cs * 2.44140625e-4f;  // 2^-12 cells
+    bool lo_z = false, hi_z = false;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const bool near_lo = valid && off[a] < eps;
         const bool near_hi = valid && (c.cs - off[a]) < eps;
-        T.lo[a] = __any_sync(0xffffffffu, near_lo) ? -2 : -1;
-        T.hi[a] = __any_sync(0xffffffffu, near_hi) ? 2 : 1;
+        if (a == 2) {
+            lo_z = near_lo;
+            hi_z = near_hi;
+        } else {
+            T.lo[a] = __any_sync(0xffffffffu, near_lo) ? -2 : -1;
+            T.hi[a] = __any_sync(0xffffffffu, near_hi) ? 2 : 1;
+        }
     }
+    tile_z_range(b, g, k0, lane, valid, lo_z, hi_z, T);
 }
 
 // Calls f(begin, end) for every stencil row of the tile, in the reference's order.  On a
@@ -149,7 +186,10 @@ __device__ __forceinline__ void for_each_row(const Buffers& b, const Geom& g, co
     // z range of every row: [z0, z1] plus, when z wraps past the end, [0, z2]
     int z0 = T.cz + T.lo[2], z1 = T.cz + T.hi[2], z2 = -1;
     int zp = -1, zq = -2;  // a wrapped piece at the front (dz < 0 past 0)
-    if (w2) {
+    if (w2 && z1 - z0 + 1 >= d2) {  // the range covers the folded axis: each cell once
+        z0 = 0;
+        z1 = d2 - 1;
+    } else if (w2) {
         if (z0 < 0) {
             zp = z0 + d2;
             zq = d2 - 1;
@@ -199,7 +239,10 @@ __device__ __forceinline__ int build_segments(const Buffers& b, const Geom& g, c
     const int d0 = g.dim[0], d1 = g.dim[1], d2 = g.dim[2];
     int z0 = T.cz + T.lo[2], z1 = T.cz + T.hi[2], z2 = -1;
     int zp = -1, zq = -2;
-    if (g.wrap[2]) {
+    if (g.wrap[2] && z1 - z0 + 1 >= d2) {  // the range covers the folded axis: each cell once
+        z0 = 0;
+        z1 = d2 - 1;
+    } else if (g.wrap[2]) {
         if (z0 < 0) {
             zp = z0 + d2;
             zq = d2 - 1;
@@ -446,6 +489,46 @@ __device__ __forceinline__ float pair_w_fast(const StepConst& c, float d2) {
         return q < 2.0f ? c.wnorm * (t2 * t2) * fmaf(2.0f, q, 1.0f) : 0.0f;
     }
     return cubic_w_fast(c, q);
+}
+
+// Precision-mode leapfrog + wall clamp on cell + offset positions (FP64 clamp).
+__device__ __forceinline__ void integrate_cells(const StepConst& c, float dt, const float* acc,
+                                                float* o, float* v, int4& cell) {
+    int* cc[3] = {&cell.x, &cell.y, &cell.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float half = 0.5f * acc[a] * dt;
+        float vv = v[a] + half;
+        float on = o[a] + vv * dt;
+        vv = vv + half;
+        v[a] = vv * c.damping;
+        if (!isfinite(on)) {  // the position is lost: park the particle as non-finite
+            cell.w = 1;
+            o[a] = on;
+            continue;
+        }
+        double X = (double)(*cc[a]) * c.cs_d + (double)on;
+        if (X < (double)c.lo[a]) {
+            X = c.lo[a];
+            v[a] = v[a] * -0.8f;
+        } else if (X > (double)c.hi[a]) {
+            X = c.hi[a];
+            v[a] = v[a] * -0.8f;
+        }
+        double f = floor(X / c.cs_d);
+        f = fmin(fmax(f, -(double)kCellClamp), (double)(kCellClamp - 1));
+        int ci = (int)f;
+        float oo = (float)(X - (double)ci * c.cs_d);
+        if (c.fp16) oo = round_half(oo);
+        if (oo >= c.cs) {
+            oo = 0.0f;
+            ci += 1;
+        } else if (oo < 0.0f) {
+            oo = 0.0f;
+        }
+        *cc[a] = ci;
+        o[a] = oo;
+    }
 }
 
 // Work distribution: warps take tiles from a per-pass counter (dynamic, so crowded cells

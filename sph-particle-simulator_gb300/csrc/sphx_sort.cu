@@ -235,29 +235,49 @@ int launch_radix_sort(const LaunchCtx& L, const Buffers& b, DevState* ds, int n)
 }
 
 // ---------------------------------------------------------------------------------------
-// tile list: a tile starts at every 32nd particle of a cell (cell-sorted order); the
-// non-finite group (key == ncells) is tiled the same way.
+// tile list: a tile starts at every tile_n-th particle of a cell, or (b.columns) of a cell
+// column (x, y, *), contiguous in cell-sorted order; the non-finite group (key == ncells)
+// is tiled the same way.  A column tile may span several cells: the passes walk the union
+// of its particles' stencils.
 // ---------------------------------------------------------------------------------------
+
+// first cell of the column of cell `key` (the non-finite group is its own column)
+__device__ __forceinline__ uint32_t column_base(uint32_t key, uint32_t k, const DevState* ds,
+                                                const uint32_t* scene_s,
+                                                const SceneInfo* scenes) {
+    if (key >= ds->ncells) return key;
+    uint32_t base = 0, d2 = (uint32_t)ds->dim[2];
+    if (scenes) {
+        const SceneInfo& sc = scenes[scene_s[k]];
+        base = sc.base;
+        d2 = (uint32_t)sc.dim[2];
+    }
+    return base + (key - base) / d2 * d2;
+}
 
 struct TileSrc {
     const uint32_t* key_s;
     const uint32_t* off;
     const DevState* ds;
+    const uint32_t* scene_s;  // batched mode (else null)
+    const SceneInfo* scenes;
     uint32_t tile_n;  // particles per tile
+    int columns;      // 1: tiles along cell columns, else within cells
     __device__ bool active() const { return !ds->status; }
     __device__ uint32_t operator()(uint32_t k) const {
-        const uint32_t st = off[key_s[k]];
+        const uint32_t key = key_s[k];
+        const uint32_t st = off[columns ? column_base(key, k, ds, scene_s, scenes) : key];
         return (k - st) % tile_n == 0 ? 1u : 0u;
     }
 };
+// Writes the tile starts and counts the occupied cells and the fullest one.
 struct TileSink {
     const uint32_t* key_s;
     const uint32_t* off;
     uint32_t* tile_start;
     DevState* ds;
     __device__ void operator()(uint32_t k, uint32_t excl, uint32_t v) const {
-        if (!v) return;
-        tile_start[excl] = k;
+        if (v) tile_start[excl] = k;
         const uint32_t c = key_s[k];
         if (c < ds->ncells && off[c] == k) {
             atomicAdd(&ds->occupied, 1u);
@@ -267,7 +287,10 @@ struct TileSink {
 };
 
 int launch_tile_scan(const LaunchCtx& L, const Buffers& b, DevState* ds, int n) {
-    return scan(L, TileSrc{b.key_s, b.off, ds, (uint32_t)b.tile_n}, TileSink{b.key_s, b.off, b.tile_start, ds},
+    const bool batched = b.nscenes > 0;
+    const TileSrc src{b.key_s, b.off, ds, batched ? b.scene_s : nullptr,
+                      batched ? b.scenes : nullptr, (uint32_t)b.tile_n, b.columns};
+    return scan(L, src, TileSink{b.key_s, b.off, b.tile_start, ds},
          (uint32_t)n, b.scan_part, &ds->n_tiles);
 }
 

@@ -1,0 +1,463 @@
+// Precision-mode neighbour passes as tile sweeps: density + pressure, and force +
+// acceleration + leapfrog + wall clamp, of the cell + offset step (compute_densities /
+// compute_pressures / compute_forces, sph_engine.cpp:203-244, 370-443; integrate_leapfrog,
+// cpp:290-310; apply_boundary_conditions, particle.cpp:122-153).
+//
+// The precision mode is judged against an FP64 evaluation, not against the reference's
+// summation order, so its passes need neither the hit lists nor the in-order folds of the
+// exact passes.  One warp owns one tile (up to 32 cell-sorted particles of one cell, one
+// per lane) and sweeps the tile's stencil 32 candidates at a time: a chunk is staged in
+// shared memory in the tile's frame, the candidates that no particle of the tile can reach
+// are culled by the tile's box, and every lane evaluates every remaining candidate against
+// its own particle, two candidates per packed FP32x2 instruction and without branches: the
+// pair's term is formed whatever the distance and is zero (or zeroed) when the candidate is
+// not a neighbour.  Every lane is busy on every instruction; the price is the terms of the
+// culled box's non-neighbours, which costs less than listing the neighbours.
+//
+// The self pair is swept like any other: its W is W(0) (the reference's m_i W(0) term) and
+// its force terms are zero (r = 0 skips the pressure term; v_i - v_i = 0).
+//
+// Smoothing kernels in the "max form" (a = max(2 - q, 0), b = max(1 - q, 0) for the cubic
+// spline), which is zero beyond the support without a test:
+//   cubic spline  W = sigma/6 (a^3 - 4 b^3),  dW/dq = sigma/2 (4 b^2 - a^2),
+//                 d2W/dq2 = sigma (a - 4 b)          (kernels.cpp:23-60, piecewise there)
+//   Wendland C2   t = max(1 - q/2, 0):  W = norm t^4 (1 + 2 q), dW/dq = -5 norm t^3 q,
+//                 laplacian = norm (5/h^2) t^2 (5 q - 3)      (kernels.cpp:172-200)
+//   Gaussian      no compact support: every term is masked by the neighbour test
+//                                                             (kernels.cpp:210-225)
+// A pair is a neighbour when |r|^2 <= r_search^2 (spatial_hash.cpp:46-50); when the search
+// radius is at least the support 2h, the max form already zeroes every non-neighbour and
+// the force sweep skips the test (kCut = false).
+#include "sphx_passes.cuh"
+
+namespace sphx {
+
+namespace {
+
+// ---- packed FP32 pairs ----------------------------------------------------------------
+struct F2 {
+    f32x2 v;
+};
+__device__ __forceinline__ F2 f2(float a) { return {pk2(a, a)}; }
+__device__ __forceinline__ F2 f2(float a, float b) { return {pk2(a, b)}; }
+__device__ __forceinline__ F2 operator+(F2 a, F2 b) { return {xadd2(a.v, b.v)}; }
+__device__ __forceinline__ F2 operator-(F2 a, F2 b) { return {xsub2(a.v, b.v)}; }
+__device__ __forceinline__ F2 operator*(F2 a, F2 b) { return {xmul2(a.v, b.v)}; }
+__device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) { return {xfma2(a.v, b.v, c.v)}; }
+__device__ __forceinline__ F2 max0(F2 a) {
+    const float2 u = upk2(a.v);
+    return f2(fmaxf(u.x, 0.0f), fmaxf(u.y, 0.0f));
+}
+__device__ __forceinline__ F2 keep(bool ka, bool kb, F2 a) {
+    const float2 u = upk2(a.v);
+    return f2(ka ? u.x : 0.0f, kb ? u.y : 0.0f);
+}
+
+// hardware square root and reciprocal square root (a few ulp; precision mode only)
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float exp_approx(float x) { return __expf(x); }
+
+// position of the empty slots of a chunk: far enough to be no particle's neighbour, near
+// enough that every term formed from it stays finite (|r|^2 of 3e30)
+constexpr float kFar = 1.0e15f;
+
+// W of two pairs (d2 = |r|^2 of each) up to the kernel's constant factor (sweep_w_scale).
+template <int K>
+__device__ __forceinline__ F2 sweep_w(const StepConst& c, F2 d2) {
+    const float2 e = upk2(d2.v);
+    if (K == SPHX_KERNEL_GAUSSIAN) return f2(exp_approx(-e.x * c.gs), exp_approx(-e.y * c.gs));
+    const F2 q = f2(sqrt_approx(e.x), sqrt_approx(e.y)) * f2(c.rcp_h);
+    if (K == SPHX_KERNEL_WENDLAND_C2) {
+        const F2 t = max0(fma2(q, f2(-0.5f), f2(1.0f)));
+        const F2 t2 = t * t;
+        return (t2 * t2) * fma2(q, f2(2.0f), f2(1.0f));
+    }
+    const F2 a = max0(f2(2.0f) - q), b = max0(f2(1.0f) - q);
+    return fma2((b * b) * b, f2(-4.0f), (a * a) * a);
+}
+__host__ __device__ __forceinline__ float sweep_w_scale(const StepConst& c) {
+    return c.kern == SPHX_KERNEL_CUBIC_SPLINE ? c.sigma * (1.0f / 6.0f) : c.wnorm;
+}
+
+// ---------------------------------------------------------------------------------------
+// density + pressure
+// ---------------------------------------------------------------------------------------
+struct SweepDensitySmem {
+    float4 box_lo, box_hi;  // the tile's box (kept here, not in registers, across the sweep)
+    int2 seg[kMaxSegments];
+    float4 xy[16];  // candidates 2p, 2p+1 of the chunk: x, x, y, y (tile frame)
+    float4 zm[16];  // z, z, m, m
+};
+
+template <int kKern>
+__global__ void __launch_bounds__(128, 8) k_density_sweep(const StepConst c, const Buffers b,
+                                                          DevState* ds) {
+    if (ds->status) return;
+    extern __shared__ __align__(16) unsigned char smem_sweep_d[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    SweepDensitySmem* S = reinterpret_cast<SweepDensitySmem*>(smem_sweep_d) + warp;
+    const uint32_t ntiles = ds->n_tiles;
+    const Geom g = grid_geom(ds);
+    const float r2 = c.r2, r2m = c.r2 * 1.0001f;
+    uint32_t my_max = 0;
+    for (uint32_t t = next_tile(&ds->work[0], lane); t < ntiles; t = next_tile(&ds->work[0], lane)) {
+        Tile T;
+        float4 xi;
+        bool valid;
+        int4 frame;
+        tile_setup_cells(c, b, g, b.tile_start[t], lane, T, xi, valid, frame);
+        const int i = T.k0 + lane;
+        {
+            const TileBox B = tile_box(xi, valid);
+            if (lane == 0) {
+                S->box_lo = make_float4(B.lo[0], B.lo[1], B.lo[2], 0.0f);
+                S->box_hi = make_float4(B.hi[0], B.hi[1], B.hi[2], 0.0f);
+            }
+        }
+        const F2 X = f2(xi.x), Y = f2(xi.y), Z = f2(xi.z);
+        KSum rk;  // sum of m_j W_ij / scale over the stencil, the particle itself included
+        uint32_t nn = 0;
+        const int nseg = build_segments(b, g, T, lane, S->seg);
+        __syncwarp();
+        for (int sg = 0; sg < nseg; ++sg) {
+            const int2 se = S->seg[sg];
+            for (int s = se.x; s < se.y; s += 32) {
+                const bool in = lane < se.y - s;
+                float4 pl = make_float4(kFar, kFar, kFar, 0.0f);
+                if (in) pl = frame_pos(b.cell4_s[s + lane], frame, b.pos4_s[s + lane], c.cs);
+                TileBox B;
+                {
+                    const float4 lo = S->box_lo, hi = S->box_hi;
+                    B.lo[0] = lo.x, B.lo[1] = lo.y, B.lo[2] = lo.z;
+                    B.hi[0] = hi.x, B.hi[1] = hi.y, B.hi[2] = hi.z;
+                }
+                const uint32_t surv = __ballot_sync(kFull, in && box_near(B, pl, r2m));
+                if (!surv) continue;
+                const int nsv = __popc(surv);
+                __syncwarp();  // the previous chunk's reads are done
+                {
+                    // survivors packed to slots 0 .. nsv-1; an odd count is padded with an
+                    // empty slot (written by lane 0 besides its own)
+                    auto put = [&](int k, const float4& v) {
+                        float* xy = reinterpret_cast<float*>(&S->xy[k >> 1]);
+                        float* zm = reinterpret_cast<float*>(&S->zm[k >> 1]);
+                        const int h = k & 1;
+                        xy[h] = v.x;
+                        xy[2 + h] = v.y;
+                        zm[h] = v.z;
+                        zm[2 + h] = v.w;
+                    };
+                    if ((surv >> lane) & 1u) put(__popc(surv & ((1u << lane) - 1u)), pl);
+                    if (lane == 0 && (nsv & 1)) put(nsv, make_float4(kFar, kFar, kFar, 0.0f));
+                }
+                __syncwarp();
+                F2 acc = f2(0.0f);
+                const int np = (nsv + 1) >> 1;
+                for (int p = 0; p < np; ++p) {
+                    const ulonglong2 u0 = *reinterpret_cast<const ulonglong2*>(&S->xy[p]);
+                    const ulonglong2 u1 = *reinterpret_cast<const ulonglong2*>(&S->zm[p]);
+                    const F2 dx = X - F2{u0.x}, dy = Y - F2{u0.y}, dz = Z - F2{u1.x};
+                    const F2 d2 = fma2(dx, dx, fma2(dy, dy, dz * dz));
+                    const float2 e = upk2(d2.v);
+                    const bool ha = e.x <= r2, hb = e.y <= r2;
+                    nn += (uint32_t)ha + (uint32_t)hb;
+                    acc = fma2(F2{u1.y}, keep(ha, hb, sweep_w<kKern>(c, d2)), acc);
+                }
+                const float2 a2 = upk2(acc.v);
+                rk.add(a2.x + a2.y);  // compensated across chunks
+            }
+        }
+        if (valid) {
+            const float rho = T.cells ? rk.value() * sweep_w_scale(c) : xmul(xi.w, c.w0);
+            const float P = xmul(c.gas, xsub(rho, c.rest));
+            // the per-candidate factors of the force sweep: (rho, P, m / (2 rho), (m / rho) mu)
+            const float mr = xdiv(xi.w, rho);
+            b.aux4_s[i] = make_float4(rho, P, 0.5f * mr, mr * c.visc);
+            my_max = max(my_max, nn);
+        }
+        __syncwarp();
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) my_max = max(my_max, __shfl_xor_sync(kFull, my_max, o));
+    if (lane == 0 && my_max) atomicMax(&ds->max_nn, (unsigned long long)my_max);
+}
+
+// ---------------------------------------------------------------------------------------
+// force + acceleration (+ leapfrog + wall clamp when kIntegrate)
+// ---------------------------------------------------------------------------------------
+struct SweepForceSmem {
+    float4 box_lo, box_hi;  // the tile's box (kept here, not in registers, across the sweep)
+    int2 seg[kMaxSegments];
+    float4 xy[16];  // candidates 2p, 2p+1: x, x, y, y (tile frame)
+    float4 zv[16];  // z, z, vx, vx
+    float4 vv[16];  // vy, vy, vz, vz
+    float4 pa[16];  // P, P, kg m/(2 rho), kg m/(2 rho)
+    float2 va[16];  // kl (m/rho) mu, kl (m/rho) mu
+};
+
+// Pressure and viscosity factors of the kernel: the force on particle t from candidate j is
+//   kg (m_j / (2 rho_j)) (P_t + P_j) G' r_vec  +  kl (m_j / rho_j) mu L' (v_j - v_t)
+// with G' and L' the kernel's gradient and Laplacian shapes below: grad W_tj = -kg G' r_vec
+// and laplacian W_tj = kl L' (r_vec = x_t - x_j).
+__host__ __device__ __forceinline__ float sweep_kg(const StepConst& c) {
+    if (c.kern == SPHX_KERNEL_GAUSSIAN) return -c.gg;
+    if (c.kern == SPHX_KERNEL_WENDLAND_C2) return 5.0f * c.wnorm * c.rcp_h;
+    return -0.5f * c.sigma * c.rcp_h;
+}
+__host__ __device__ __forceinline__ float sweep_kl(const StepConst& c) {
+    if (c.kern == SPHX_KERNEL_GAUSSIAN) return c.gl;
+    if (c.kern == SPHX_KERNEL_WENDLAND_C2) return c.wl;
+    return c.sigma * c.rcp_hsq;
+}
+
+// One packed pair of candidates against the lane's particle; F accumulates.  kMask: zero
+// the terms of non-neighbours by selection (needed when the search radius is below the
+// support, for the Gaussian, and when a staged candidate carries a non-finite velocity or
+// factor, which a zero factor would not cancel).
+template <int K, bool kMask>
+__device__ __forceinline__ void sweep_force_pair(const StepConst& c, F2 X, F2 Y, F2 Z, F2 VX,
+                                                 F2 VY, F2 VZ, F2 PT, const SweepForceSmem* S,
+                                                 int p, F2& Fx, F2& Fy, F2& Fz) {
+    const ulonglong2 u0 = *reinterpret_cast<const ulonglong2*>(&S->xy[p]);
+    const ulonglong2 u1 = *reinterpret_cast<const ulonglong2*>(&S->zv[p]);
+    const ulonglong2 u2 = *reinterpret_cast<const ulonglong2*>(&S->vv[p]);
+    const ulonglong2 u3 = *reinterpret_cast<const ulonglong2*>(&S->pa[p]);
+    const F2 va{*reinterpret_cast<const f32x2*>(&S->va[p])};
+    const F2 dx = X - F2{u0.x}, dy = Y - F2{u0.y}, dz = Z - F2{u1.x};
+    const F2 d2 = fma2(dx, dx, fma2(dy, dy, dz * dz));
+    const float2 e = upk2(d2.v);
+    // 1/|r|, or 0 where the reference skips the pressure term (|r| < 1e-6)
+    const F2 R = f2(e.x >= 1e-12f ? rsqrt_approx(e.x) : 0.0f, e.y >= 1e-12f ? rsqrt_approx(e.y) : 0.0f);
+    F2 G, L;
+    if (K == SPHX_KERNEL_GAUSSIAN) {
+        const F2 ex = f2(exp_approx(-e.x * c.gs), exp_approx(-e.y * c.gs));
+        G = keep(e.x >= 1e-12f, e.y >= 1e-12f, ex);
+        L = ex * fma2(d2, f2(c.g2s), f2(-3.0f));
+    } else {
+        const F2 q = (d2 * R) * f2(c.rcp_h);
+        if (K == SPHX_KERNEL_WENDLAND_C2) {
+            const F2 t = max0(fma2(q, f2(-0.5f), f2(1.0f)));
+            const F2 t2 = t * t;
+            G = ((t2 * t) * q) * R;
+            L = t2 * fma2(q, f2(5.0f), f2(-3.0f));
+        } else {
+            const F2 a = max0(f2(2.0f) - q), bb = max0(f2(1.0f) - q);
+            const F2 b2 = bb + bb;
+            G = ((b2 - a) * (b2 + a)) * R;  // 4 b^2 - a^2
+            L = fma2(bb, f2(-4.0f), a);     // a - 4 b
+        }
+    }
+    F2 cp = (PT + F2{u3.x}) * F2{u3.y} * G;
+    F2 cv = va * L;
+    F2 dvx = F2{u1.y} - VX, dvy = F2{u2.x} - VY, dvz = F2{u2.y} - VZ;
+    if (kMask) {
+        const bool ha = e.x <= c.r2, hb = e.y <= c.r2;
+        cp = keep(ha, hb, cp);
+        cv = keep(ha, hb, cv);
+        dvx = keep(ha, hb, dvx);
+        dvy = keep(ha, hb, dvy);
+        dvz = keep(ha, hb, dvz);
+    }
+    Fx = fma2(cv, dvx, fma2(cp, dx, Fx));
+    Fy = fma2(cv, dvy, fma2(cp, dy, Fy));
+    Fz = fma2(cv, dvz, fma2(cp, dz, Fz));
+}
+
+template <bool kIntegrate, int kKern, bool kCut>
+__global__ void __launch_bounds__(128, 6) k_force_sweep(const StepConst c, const Buffers b,
+                                                        DevState* ds) {
+    if (ds->status) return;
+    extern __shared__ __align__(16) unsigned char smem_sweep_f[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    SweepForceSmem* S = reinterpret_cast<SweepForceSmem*>(smem_sweep_f) + warp;
+    const uint32_t ntiles = ds->n_tiles;
+    const Geom g = grid_geom(ds);
+    const float r2m = c.r2 * 1.0001f;
+    const float kg = sweep_kg(c), kl = sweep_kl(c);
+    for (uint32_t t = next_tile(&ds->work[1], lane); t < ntiles; t = next_tile(&ds->work[1], lane)) {
+        Tile T;
+        float4 xi;
+        bool valid;
+        int4 frame;
+        tile_setup_cells(c, b, g, b.tile_start[t], lane, T, xi, valid, frame);
+        const int i = T.k0 + lane;
+        {
+            const TileBox B = tile_box(xi, valid);
+            if (lane == 0) {
+                S->box_lo = make_float4(B.lo[0], B.lo[1], B.lo[2], 0.0f);
+                S->box_hi = make_float4(B.hi[0], B.hi[1], B.hi[2], 0.0f);
+            }
+        }
+        F2 VX, VY, VZ, PT;
+        {
+            const float4 vi = valid ? b.vel4_s[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float Pi = valid ? b.aux4_s[i].y : 0.0f;
+            VX = f2(vi.x), VY = f2(vi.y), VZ = f2(vi.z), PT = f2(Pi);
+        }
+        const F2 X = f2(xi.x), Y = f2(xi.y), Z = f2(xi.z);
+        KSum Sx, Sy, Sz;  // force sums, compensated across chunks
+        const int nseg = build_segments(b, g, T, lane, S->seg);
+        __syncwarp();
+        for (int sg = 0; sg < nseg; ++sg) {
+            const int2 se = S->seg[sg];
+            for (int s = se.x; s < se.y; s += 32) {
+                const bool in = lane < se.y - s;
+                float4 pl = make_float4(kFar, kFar, kFar, 0.0f);
+                if (in) pl = frame_pos(b.cell4_s[s + lane], frame, b.pos4_s[s + lane], c.cs);
+                TileBox B;
+                {
+                    const float4 lo = S->box_lo, hi = S->box_hi;
+                    B.lo[0] = lo.x, B.lo[1] = lo.y, B.lo[2] = lo.z;
+                    B.hi[0] = hi.x, B.hi[1] = hi.y, B.hi[2] = hi.z;
+                }
+                const uint32_t surv = __ballot_sync(kFull, in && box_near(B, pl, r2m));
+                if (!surv) continue;
+                const int nsv = __popc(surv);
+                const bool mine = (surv >> lane) & 1u;
+                float4 vl = make_float4(0.f, 0.f, 0.f, 0.f), al = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (mine) {
+                    vl = b.vel4_s[s + lane];
+                    al = b.aux4_s[s + lane];
+                }
+                const float cpf = kg * al.z, cvf = kl * al.w;
+                // a non-finite velocity or factor is not cancelled by a zero factor: such a
+                // chunk takes the masked sweep
+                const bool odd = !isfinite(vl.x + vl.y + vl.z + al.y + cpf + cvf);
+                const bool masked = kCut || __any_sync(kFull, odd);
+                __syncwarp();  // the previous chunk's reads are done
+                // survivors packed to slots 0 .. nsv-1; an odd count is padded with an empty
+                // slot (written by lane 0 besides its own)
+                auto put = [&](int k, const float4& x, const float4& v, const float4& a3) {
+                    const int p = k >> 1, h = k & 1;
+                    float* xy = reinterpret_cast<float*>(&S->xy[p]);
+                    float* zv = reinterpret_cast<float*>(&S->zv[p]);
+                    float* vv = reinterpret_cast<float*>(&S->vv[p]);
+                    float* pa = reinterpret_cast<float*>(&S->pa[p]);
+                    float* va = reinterpret_cast<float*>(&S->va[p]);
+                    xy[h] = x.x;
+                    xy[2 + h] = x.y;
+                    zv[h] = x.z;
+                    zv[2 + h] = v.x;
+                    vv[h] = v.y;
+                    vv[2 + h] = v.z;
+                    pa[h] = a3.x;
+                    pa[2 + h] = a3.y;
+                    va[h] = a3.z;
+                };
+                if (mine)
+                    put(__popc(surv & ((1u << lane) - 1u)), pl, vl, make_float4(al.y, cpf, cvf, 0.f));
+                if (lane == 0 && (nsv & 1)) {
+                    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+                    put(nsv, make_float4(kFar, kFar, kFar, 0.0f), z, z);
+                }
+                __syncwarp();
+                F2 Fx = f2(0.0f), Fy = f2(0.0f), Fz = f2(0.0f);
+                const int np = (nsv + 1) >> 1;
+                if (masked) {
+                    for (int p = 0; p < np; ++p)
+                        sweep_force_pair<kKern, true>(c, X, Y, Z, VX, VY, VZ, PT, S, p, Fx, Fy, Fz);
+                } else {
+                    for (int p = 0; p < np; ++p)
+                        sweep_force_pair<kKern, false>(c, X, Y, Z, VX, VY, VZ, PT, S, p, Fx, Fy, Fz);
+                }
+                const float2 fx = upk2(Fx.v), fy = upk2(Fy.v), fz = upk2(Fz.v);
+                Sx.add(fx.x + fx.y);
+                Sy.add(fy.x + fy.y);
+                Sz.add(fz.x + fz.y);
+            }
+        }
+        __syncwarp();
+        if (!valid) continue;
+        const float mi = xi.w;
+        const float ax = Sx.value() / mi;
+        const float ay = (Sy.value() + c.grav * mi) / mi;
+        const float az = Sz.value() / mi;
+        b.acc4_s[i] = make_float4(ax, ay, az, 0.0f);
+        if (!kIntegrate) continue;
+        const uint32_t id = b.id_s[i];
+        int4 cell = b.cell4_s[i];
+        const float4 own = b.pos4_s[i];
+        const float4 vi = b.vel4_s[i];  // loaded again: not held across the sweep
+        float o[3] = {own.x, own.y, own.z}, v[3] = {vi.x, vi.y, vi.z};
+        const float acc[3] = {ax, ay, az};
+        if (!cell.w) integrate_cells(c, ds->dt, acc, o, v, cell);
+        b.cell4[id] = cell;
+        b.pos4[id] = make_float4(o[0], o[1], o[2], mi);
+        b.vel4[id] = make_float4(v[0], v[1], v[2], 0.0f);
+        if (id == 0) {
+            ds->a0[0] = ax;
+            ds->a0[1] = ay;
+            ds->a0[2] = az;
+        }
+    }
+}
+
+template <class K>
+void launch_sweep(const LaunchCtx& L, LaunchShapeCache& cache, K kernel, size_t smem_per_warp,
+                  const StepConst& c, const Buffers& b, DevState* ds) {
+    const int threads = 32 * L.warps_per_block;
+    const size_t sm = (size_t)L.warps_per_block * smem_per_warp;
+    const int nb = cached_resident_blocks(cache, L, kernel, threads, sm);
+    kernel<<<nb, threads, sm, L.stream>>>(c, b, ds);
+}
+
+template <int kKern>
+void launch_density_sweep_k(const LaunchCtx& L, const StepConst& c, const Buffers& b,
+                            DevState* ds) {
+    static LaunchShapeCache cache;
+    launch_sweep(L, cache, k_density_sweep<kKern>, sizeof(SweepDensitySmem), c, b, ds);
+}
+
+template <bool kIntegrate, int kKern, bool kCut>
+void launch_force_sweep_v(const LaunchCtx& L, const StepConst& c, const Buffers& b,
+                          DevState* ds) {
+    static LaunchShapeCache cache;
+    launch_sweep(L, cache, k_force_sweep<kIntegrate, kKern, kCut>, sizeof(SweepForceSmem), c, b,
+                 ds);
+}
+
+template <int kKern>
+void launch_force_sweep_k(const LaunchCtx& L, const StepConst& c, const Buffers& b,
+                          DevState* ds, int integrate) {
+    // the max form zeroes every pair beyond the support 2h; a search radius below it needs
+    // the neighbour test (the Gaussian has no compact support)
+    const bool cut = kKern == SPHX_KERNEL_GAUSSIAN || c.r2 < 4.0f * c.h_sq;
+    if (integrate) {
+        if (cut) launch_force_sweep_v<true, kKern, true>(L, c, b, ds);
+        else launch_force_sweep_v<true, kKern, false>(L, c, b, ds);
+    } else {
+        if (cut) launch_force_sweep_v<false, kKern, true>(L, c, b, ds);
+        else launch_force_sweep_v<false, kKern, false>(L, c, b, ds);
+    }
+}
+
+}  // namespace
+
+int launch_density_sweep(const LaunchCtx& L, const StepConst& c, const Buffers& b,
+                         DevState* ds) {
+    if (c.kern == SPHX_KERNEL_WENDLAND_C2) launch_density_sweep_k<SPHX_KERNEL_WENDLAND_C2>(L, c, b, ds);
+    else if (c.kern == SPHX_KERNEL_GAUSSIAN) launch_density_sweep_k<SPHX_KERNEL_GAUSSIAN>(L, c, b, ds);
+    else launch_density_sweep_k<SPHX_KERNEL_CUBIC_SPLINE>(L, c, b, ds);
+    return 1;
+}
+
+int launch_force_sweep(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds,
+                       int integrate) {
+    if (c.kern == SPHX_KERNEL_WENDLAND_C2)
+        launch_force_sweep_k<SPHX_KERNEL_WENDLAND_C2>(L, c, b, ds, integrate);
+    else if (c.kern == SPHX_KERNEL_GAUSSIAN)
+        launch_force_sweep_k<SPHX_KERNEL_GAUSSIAN>(L, c, b, ds, integrate);
+    else launch_force_sweep_k<SPHX_KERNEL_CUBIC_SPLINE>(L, c, b, ds, integrate);
+    return 1;
+}
+
+}  // namespace sphx

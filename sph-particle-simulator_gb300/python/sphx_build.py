@@ -26,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
               "-ffp-contract=off", "-Xptxas", "-warn-spills", f"-I{REPO / 'include'}"]
 CUDA_SOURCES = ["sphx_sort.cu", "sphx_grid.cu", "sphx_passes.cu", "sphx_density.cu",
-                "sphx_force.cu", "sphx_batch.cu",
+                "sphx_force.cu", "sphx_sweep.cu", "sphx_batch.cu",
                 "sphx_capi.cu", "sphx_hash.cu", "sphx_noalloc.cu",
                 "sphx_render.cu", "sphx_gen.cu"]
 
