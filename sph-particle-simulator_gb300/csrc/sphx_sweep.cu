@@ -28,6 +28,12 @@
 // A pair is a neighbour when |r|^2 <= r_search^2 (spatial_hash.cpp:46-50); when the search
 // radius is at least the support 2h, the max form already zeroes every non-neighbour and
 // the force sweep skips the test (kCut = false).
+//
+// Positions are swept in units of h (the tile's frame scaled by 1/h): |r|/h = q comes
+// without a multiplication, and every force term that needs the direction uses r_vec / |r|,
+// which is the same in any unit.  The pressure term of a pair closer than 1e-6 m, which the
+// reference skips, is formed here (it is at most |grad W| 1e-6 m, far below the stated
+// bound; a coincident pair, |r| = 0, gives exactly 0 as in the reference).
 #include "sphx_passes.cuh"
 
 namespace sphx {
@@ -70,12 +76,32 @@ __device__ __forceinline__ float exp_approx(float x) { return __expf(x); }
 // enough that every term formed from it stays finite (|r|^2 of 3e30)
 constexpr float kFar = 1.0e15f;
 
-// W of two pairs (d2 = |r|^2 of each) up to the kernel's constant factor (sweep_w_scale).
+// The sweeps' lengths in units of h.
+struct SweepUnits {
+    float inv;   // 1/h: metres -> sweep units
+    float r2;    // r_search^2 / h^2: the neighbour test
+    float r2m;   // the same with the box cull's margin
+    float skip2; // (1e-6 m / h)^2: the Gaussian's pressure-term skip
+};
+__device__ __forceinline__ SweepUnits sweep_units(const StepConst& c) {
+    SweepUnits u;
+    u.inv = c.rcp_h;
+    u.r2 = c.r2 * c.rcp_hsq;
+    u.r2m = u.r2 * 1.0001f;
+    u.skip2 = 1e-12f * c.rcp_hsq;
+    return u;
+}
+__device__ __forceinline__ float4 scaled(const float4& x, float inv) {
+    return make_float4(x.x * inv, x.y * inv, x.z * inv, x.w);
+}
+
+// W of two pairs (d2 = (|r|/h)^2 of each) up to the kernel's constant factor
+// (sweep_w_scale); the Gaussian's exp(-|r|^2 / h^2) is exp(-d2).
 template <int K>
 __device__ __forceinline__ F2 sweep_w(const StepConst& c, F2 d2) {
     const float2 e = upk2(d2.v);
-    if (K == SPHX_KERNEL_GAUSSIAN) return f2(exp_approx(-e.x * c.gs), exp_approx(-e.y * c.gs));
-    const F2 q = f2(sqrt_approx(e.x), sqrt_approx(e.y)) * f2(c.rcp_h);
+    if (K == SPHX_KERNEL_GAUSSIAN) return f2(exp_approx(-e.x), exp_approx(-e.y));
+    const F2 q = f2(sqrt_approx(e.x), sqrt_approx(e.y));
     if (K == SPHX_KERNEL_WENDLAND_C2) {
         const F2 t = max0(fma2(q, f2(-0.5f), f2(1.0f)));
         const F2 t2 = t * t;
@@ -99,7 +125,7 @@ struct SweepDensitySmem {
 };
 
 template <int kKern>
-__global__ void __launch_bounds__(128, 8) k_density_sweep(const StepConst c, const Buffers b,
+__global__ void __launch_bounds__(128, 7) k_density_sweep(const StepConst c, const Buffers b,
                                                           DevState* ds) {
     if (ds->status) return;
     extern __shared__ __align__(16) unsigned char smem_sweep_d[];
@@ -107,7 +133,7 @@ __global__ void __launch_bounds__(128, 8) k_density_sweep(const StepConst c, con
     SweepDensitySmem* S = reinterpret_cast<SweepDensitySmem*>(smem_sweep_d) + warp;
     const uint32_t ntiles = ds->n_tiles;
     const Geom g = grid_geom(ds);
-    const float r2 = c.r2, r2m = c.r2 * 1.0001f;
+    const SweepUnits U = sweep_units(c);
     uint32_t my_max = 0;
     for (uint32_t t = next_tile(&ds->work[0], lane); t < ntiles; t = next_tile(&ds->work[0], lane)) {
         Tile T;
@@ -116,6 +142,7 @@ __global__ void __launch_bounds__(128, 8) k_density_sweep(const StepConst c, con
         int4 frame;
         tile_setup_cells(c, b, g, b.tile_start[t], lane, T, xi, valid, frame);
         const int i = T.k0 + lane;
+        xi = scaled(xi, U.inv);
         {
             const TileBox B = tile_box(xi, valid);
             if (lane == 0) {
@@ -133,14 +160,14 @@ __global__ void __launch_bounds__(128, 8) k_density_sweep(const StepConst c, con
             for (int s = se.x; s < se.y; s += 32) {
                 const bool in = lane < se.y - s;
                 float4 pl = make_float4(kFar, kFar, kFar, 0.0f);
-                if (in) pl = frame_pos(b.cell4_s[s + lane], frame, b.pos4_s[s + lane], c.cs);
+                if (in) pl = scaled(frame_pos(b.cell4_s[s + lane], frame, b.pos4_s[s + lane], c.cs), U.inv);
                 TileBox B;
                 {
                     const float4 lo = S->box_lo, hi = S->box_hi;
                     B.lo[0] = lo.x, B.lo[1] = lo.y, B.lo[2] = lo.z;
                     B.hi[0] = hi.x, B.hi[1] = hi.y, B.hi[2] = hi.z;
                 }
-                const uint32_t surv = __ballot_sync(kFull, in && box_near(B, pl, r2m));
+                const uint32_t surv = __ballot_sync(kFull, in && box_near(B, pl, U.r2m));
                 if (!surv) continue;
                 const int nsv = __popc(surv);
                 __syncwarp();  // the previous chunk's reads are done
@@ -168,7 +195,7 @@ __global__ void __launch_bounds__(128, 8) k_density_sweep(const StepConst c, con
                     const F2 dx = X - F2{u0.x}, dy = Y - F2{u0.y}, dz = Z - F2{u1.x};
                     const F2 d2 = fma2(dx, dx, fma2(dy, dy, dz * dz));
                     const float2 e = upk2(d2.v);
-                    const bool ha = e.x <= r2, hb = e.y <= r2;
+                    const bool ha = e.x <= U.r2, hb = e.y <= U.r2;
                     nn += (uint32_t)ha + (uint32_t)hb;
                     acc = fma2(F2{u1.y}, keep(ha, hb, sweep_w<kKern>(c, d2)), acc);
                 }
@@ -207,9 +234,9 @@ struct SweepForceSmem {
 // Pressure and viscosity factors of the kernel: the force on particle t from candidate j is
 //   kg (m_j / (2 rho_j)) (P_t + P_j) G' r_vec  +  kl (m_j / rho_j) mu L' (v_j - v_t)
 // with G' and L' the kernel's gradient and Laplacian shapes below: grad W_tj = -kg G' r_vec
-// and laplacian W_tj = kl L' (r_vec = x_t - x_j).
+// and laplacian W_tj = kl L' (r_vec = x_t - x_j, in units of h).
 __host__ __device__ __forceinline__ float sweep_kg(const StepConst& c) {
-    if (c.kern == SPHX_KERNEL_GAUSSIAN) return -c.gg;
+    if (c.kern == SPHX_KERNEL_GAUSSIAN) return -c.gg * c.h;  // G' r_vec in h units
     if (c.kern == SPHX_KERNEL_WENDLAND_C2) return 5.0f * c.wnorm * c.rcp_h;
     return -0.5f * c.sigma * c.rcp_h;
 }
@@ -224,7 +251,7 @@ __host__ __device__ __forceinline__ float sweep_kl(const StepConst& c) {
 // support, for the Gaussian, and when a staged candidate carries a non-finite velocity or
 // factor, which a zero factor would not cancel).
 template <int K, bool kMask>
-__device__ __forceinline__ void sweep_force_pair(const StepConst& c, F2 X, F2 Y, F2 Z, F2 VX,
+__device__ __forceinline__ void sweep_force_pair(const SweepUnits& U, F2 X, F2 Y, F2 Z, F2 VX,
                                                  F2 VY, F2 VZ, F2 PT, const SweepForceSmem* S,
                                                  int p, F2& Fx, F2& Fy, F2& Fz) {
     const ulonglong2 u0 = *reinterpret_cast<const ulonglong2*>(&S->xy[p]);
@@ -235,32 +262,34 @@ __device__ __forceinline__ void sweep_force_pair(const StepConst& c, F2 X, F2 Y,
     const F2 dx = X - F2{u0.x}, dy = Y - F2{u0.y}, dz = Z - F2{u1.x};
     const F2 d2 = fma2(dx, dx, fma2(dy, dy, dz * dz));
     const float2 e = upk2(d2.v);
-    // 1/|r|, or 0 where the reference skips the pressure term (|r| < 1e-6)
-    const F2 R = f2(e.x >= 1e-12f ? rsqrt_approx(e.x) : 0.0f, e.y >= 1e-12f ? rsqrt_approx(e.y) : 0.0f);
     F2 G, L;
     if (K == SPHX_KERNEL_GAUSSIAN) {
-        const F2 ex = f2(exp_approx(-e.x * c.gs), exp_approx(-e.y * c.gs));
-        G = keep(e.x >= 1e-12f, e.y >= 1e-12f, ex);
-        L = ex * fma2(d2, f2(c.g2s), f2(-3.0f));
+        const F2 ex = f2(exp_approx(-e.x), exp_approx(-e.y));
+        G = keep(e.x >= U.skip2, e.y >= U.skip2, ex);
+        L = ex * fma2(d2, f2(2.0f), f2(-3.0f));  // 2 |r|^2 / h^2 - 3
     } else {
-        const F2 q = (d2 * R) * f2(c.rcp_h);
+        // 1/|r| (h units); a coincident pair gets a finite value and q = 0, where the
+        // gradient shapes below are 0
+        const F2 dd = d2 + f2(1e-30f);
+        const float2 de = upk2(dd.v);
+        const F2 R = f2(rsqrt_approx(de.x), rsqrt_approx(de.y));
+        const F2 q = d2 * R;
         if (K == SPHX_KERNEL_WENDLAND_C2) {
             const F2 t = max0(fma2(q, f2(-0.5f), f2(1.0f)));
             const F2 t2 = t * t;
             G = ((t2 * t) * q) * R;
             L = t2 * fma2(q, f2(5.0f), f2(-3.0f));
         } else {
-            const F2 a = max0(f2(2.0f) - q), bb = max0(f2(1.0f) - q);
-            const F2 b2 = bb + bb;
+            const F2 a = max0(f2(2.0f) - q), b2 = max0(fma2(q, f2(-2.0f), f2(2.0f)));  // b2 = 2b
             G = ((b2 - a) * (b2 + a)) * R;  // 4 b^2 - a^2
-            L = fma2(bb, f2(-4.0f), a);     // a - 4 b
+            L = fma2(b2, f2(-2.0f), a);     // a - 4 b
         }
     }
     F2 cp = (PT + F2{u3.x}) * F2{u3.y} * G;
     F2 cv = va * L;
     F2 dvx = F2{u1.y} - VX, dvy = F2{u2.x} - VY, dvz = F2{u2.y} - VZ;
     if (kMask) {
-        const bool ha = e.x <= c.r2, hb = e.y <= c.r2;
+        const bool ha = e.x <= U.r2, hb = e.y <= U.r2;
         cp = keep(ha, hb, cp);
         cv = keep(ha, hb, cv);
         dvx = keep(ha, hb, dvx);
@@ -281,7 +310,7 @@ __global__ void __launch_bounds__(128, 6) k_force_sweep(const StepConst c, const
     SweepForceSmem* S = reinterpret_cast<SweepForceSmem*>(smem_sweep_f) + warp;
     const uint32_t ntiles = ds->n_tiles;
     const Geom g = grid_geom(ds);
-    const float r2m = c.r2 * 1.0001f;
+    const SweepUnits U = sweep_units(c);
     const float kg = sweep_kg(c), kl = sweep_kl(c);
     for (uint32_t t = next_tile(&ds->work[1], lane); t < ntiles; t = next_tile(&ds->work[1], lane)) {
         Tile T;
@@ -290,6 +319,7 @@ __global__ void __launch_bounds__(128, 6) k_force_sweep(const StepConst c, const
         int4 frame;
         tile_setup_cells(c, b, g, b.tile_start[t], lane, T, xi, valid, frame);
         const int i = T.k0 + lane;
+        xi = scaled(xi, U.inv);
         {
             const TileBox B = tile_box(xi, valid);
             if (lane == 0) {
@@ -312,14 +342,14 @@ __global__ void __launch_bounds__(128, 6) k_force_sweep(const StepConst c, const
             for (int s = se.x; s < se.y; s += 32) {
                 const bool in = lane < se.y - s;
                 float4 pl = make_float4(kFar, kFar, kFar, 0.0f);
-                if (in) pl = frame_pos(b.cell4_s[s + lane], frame, b.pos4_s[s + lane], c.cs);
+                if (in) pl = scaled(frame_pos(b.cell4_s[s + lane], frame, b.pos4_s[s + lane], c.cs), U.inv);
                 TileBox B;
                 {
                     const float4 lo = S->box_lo, hi = S->box_hi;
                     B.lo[0] = lo.x, B.lo[1] = lo.y, B.lo[2] = lo.z;
                     B.hi[0] = hi.x, B.hi[1] = hi.y, B.hi[2] = hi.z;
                 }
-                const uint32_t surv = __ballot_sync(kFull, in && box_near(B, pl, r2m));
+                const uint32_t surv = __ballot_sync(kFull, in && box_near(B, pl, U.r2m));
                 if (!surv) continue;
                 const int nsv = __popc(surv);
                 const bool mine = (surv >> lane) & 1u;
@@ -364,10 +394,10 @@ __global__ void __launch_bounds__(128, 6) k_force_sweep(const StepConst c, const
                 const int np = (nsv + 1) >> 1;
                 if (masked) {
                     for (int p = 0; p < np; ++p)
-                        sweep_force_pair<kKern, true>(c, X, Y, Z, VX, VY, VZ, PT, S, p, Fx, Fy, Fz);
+                        sweep_force_pair<kKern, true>(U, X, Y, Z, VX, VY, VZ, PT, S, p, Fx, Fy, Fz);
                 } else {
                     for (int p = 0; p < np; ++p)
-                        sweep_force_pair<kKern, false>(c, X, Y, Z, VX, VY, VZ, PT, S, p, Fx, Fy, Fz);
+                        sweep_force_pair<kKern, false>(U, X, Y, Z, VX, VY, VZ, PT, S, p, Fx, Fy, Fz);
                 }
                 const float2 fx = upk2(Fx.v), fy = upk2(Fy.v), fz = upk2(Fz.v);
                 Sx.add(fx.x + fx.y);
