@@ -29,8 +29,8 @@ constexpr uint32_t kDenseOccupancy = 128;
 // kDense: the variant with the dense-chunk path.  Both variants are launched every step;
 // each returns at once unless the grid's fullest cell says the state is its case, so the
 // lattice-like states run the leaner code and the collapsed ones get the dense path.
-template <bool kPrecise, bool kBatch, int kKern, bool kNZ, bool kDense>
-__global__ void __launch_bounds__(128, kDense || kPrecise ? 9 : 10) k_density(
+template <bool kBatch, int kKern, bool kNZ, bool kDense>
+__global__ void __launch_bounds__(128, kDense ? 9 : 10) k_density(
     const StepConst cp, const Buffers b, DevState* ds) {
     if (ds->status) return;
     if (kDense != (ds->max_occ > kDenseOccupancy)) return;
@@ -58,9 +58,7 @@ __global__ void __launch_bounds__(128, kDense || kPrecise ? 9 : 10) k_density(
         Tile T;
         float4 xi;
         bool valid;
-        int4 frame = make_int4(0, 0, 0, 0);
-        if (kPrecise) tile_setup_cells(c, b, g, k0, lane, T, xi, valid, frame);
-        else tile_setup(c, b, g, k0, lane, T, xi, valid);
+        tile_setup(c, b, g, k0, lane, T, xi, valid);
         const int i = T.k0 + lane;
         {
             const TileBox B = tile_box(xi, valid);
@@ -71,8 +69,6 @@ __global__ void __launch_bounds__(128, kDense || kPrecise ? 9 : 10) k_density(
         }
         S->tpos[lane] = xi;
         float rho = xmul(xi.w, c.w0);
-        KSum rk;
-        rk.s = rho;
         uint32_t nn = 0;
         // hit-mask records of this tile: from the warp's cursor on, one per chunk
         __syncwarp();
@@ -86,14 +82,11 @@ __global__ void __launch_bounds__(128, kDense || kPrecise ? 9 : 10) k_density(
             for (int s = a; s < e; s += kTile, ++nrec) {
                 const int m = min(kTile, e - s);
                 __syncwarp();
-                float4 pl = lane < m ? b.pos4_s[s + lane] : make_float4(inf, inf, inf, 0.f);
-                if (kPrecise && lane < m) pl = frame_pos(b.cell4_s[s + lane], frame, pl, c.cs);
+                const float4 pl = lane < m ? b.pos4_s[s + lane] : make_float4(inf, inf, inf, 0.f);
                 S->cand[lane] = pl;
-                if (!kPrecise) {
-                    S->cx[lane] = pl.x;
-                    S->cy[lane] = pl.y;
-                    S->cz[lane] = pl.z;
-                }
+                S->cx[lane] = pl.x;
+                S->cy[lane] = pl.y;
+                S->cz[lane] = pl.z;
                 TileBox B;
                 {
                     const float4 lo = S->box_lo, hi = S->box_hi;
@@ -110,8 +103,7 @@ __global__ void __launch_bounds__(128, kDense || kPrecise ? 9 : 10) k_density(
                     continue;
                 }
                 uint32_t mask = 0u;
-                if (valid) mask = kPrecise ? chunk_hits<true>(S->cand, surv, xi, c.r2)
-                                           : chunk_hits_x2(S->cx, S->cy, S->cz, surv, xi, c.r2);
+                if (valid) mask = chunk_hits_x2(S->cx, S->cy, S->cz, surv, xi, c.r2);
                 if (rec) __stcs(rec, mask);
                 nn += __popc(mask);
                 const int self = i - s;
@@ -126,47 +118,28 @@ __global__ void __launch_bounds__(128, kDense || kPrecise ? 9 : 10) k_density(
                 // terms and additions, without the hit list and the lane-by-lane fold.
                 const int lo = max(T.k0, s), hi = min(T.k0 + T.cnt, s + m);
                 if (kDense && H == (uint32_t)(T.cnt * m - max(hi - lo, 0))) {
-                    float part = 0.0f;
                     for (int jj = 0; jj < m; ++jj) {
                         if (!valid || jj == self) continue;
                         const float4 xj = S->cand[jj];
-                        if (kPrecise) {
-                            const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-                            part += xj.w * pair_w_fast<kKern>(c, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-                        } else {
-                            rho = xadd(rho, xmul(xj.w, pair_w_exact<kKern, kNZ>(c, diff_d2(xi, xj))));
-                        }
+                        rho = xadd(rho, xmul(xj.w, pair_w_exact<kKern, kNZ>(c, diff_d2(xi, xj))));
                     }
-                    if (kPrecise) rk.add(part);
                     continue;
                 }
                 list_hits(S->plist, mask, o, lane);
                 __syncwarp();
-                float part = 0.0f;  // precision mode: this chunk's terms, one FP32 sum
                 for (uint32_t base = 0; base < H; base += kDensityBatch) {
                     const uint32_t end = min(H, base + kDensityBatch);
                     for (uint32_t f = base + lane; f < end; f += 32) {
                         const uint32_t pr = S->plist[f];
                         const float4 xj = S->cand[pr & 31];
-                        if (kPrecise) {
-                            const float4 xt = S->tpos[pr >> 5];
-                            const float dx = xt.x - xj.x, dy = xt.y - xj.y, dz = xt.z - xj.z;
-                            S->tbuf[f - base] =
-                                xj.w * pair_w_fast<kKern>(c, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-                        } else {
-                            const float d2 = diff_d2(S->tpos[pr >> 5], xj);
-                            S->tbuf[f - base] = xmul(xj.w, pair_w_exact<kKern, kNZ>(c, d2));
-                        }
+                        const float d2 = diff_d2(S->tpos[pr >> 5], xj);
+                        S->tbuf[f - base] = xmul(xj.w, pair_w_exact<kKern, kNZ>(c, d2));
                     }
                     __syncwarp();
                     const uint32_t k1 = min(o + cnt, end);
-                    if (kPrecise)
-                        for (uint32_t k = max(o, base); k < k1; ++k) part += S->tbuf[k - base];
-                    else
-                        for (uint32_t k = max(o, base); k < k1; ++k) rho = xadd(rho, S->tbuf[k - base]);
+                    for (uint32_t k = max(o, base); k < k1; ++k) rho = xadd(rho, S->tbuf[k - base]);
                     __syncwarp();
                 }
-                if (kPrecise) rk.add(part);  // compensated across chunks
             }
         }
         if (b.hitmask && lane == 0) {
@@ -175,14 +148,11 @@ __global__ void __launch_bounds__(128, kDense || kPrecise ? 9 : 10) k_density(
             if (fits) S->mcur = slot + nrec;
         }
         if (valid) {
-            if (kPrecise) rho = rk.value();
             const float P = xmul(c.gas, xsub(rho, c.rest));
             // the per-candidate factors of the force pass's pair terms, each formed once here
-            // with the rounding the reference applies per pair: exact mode (rho, P, 2 rho,
-            // (m / rho) mu); precision mode (rho, P, m / (2 rho), (m / rho) mu)
+            // with the rounding the reference applies per pair: (rho, P, 2 rho, (m / rho) mu)
             const float mr = xdiv(xi.w, rho);
-            b.aux4_s[i] = kPrecise ? make_float4(rho, P, 0.5f * mr, mr * c.visc)
-                                   : make_float4(rho, P, xmul(2.0f, rho), xmul(mr, c.visc));
+            b.aux4_s[i] = make_float4(rho, P, xmul(2.0f, rho), xmul(mr, c.visc));
             my_max = max(my_max, nn);
         }
         __syncwarp();
@@ -192,22 +162,22 @@ __global__ void __launch_bounds__(128, kDense || kPrecise ? 9 : 10) k_density(
     if (lane == 0 && my_max) atomicMax(&ds->max_nn, (unsigned long long)my_max);
 }
 
-template <bool kPrecise, bool kBatch, int kKern, bool kNZ, bool kDense>
+template <bool kBatch, int kKern, bool kNZ, bool kDense>
 static void launch_density_v(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                              DevState* ds) {
     const int threads = 32 * L.warps_per_block;
     const size_t sm = (size_t)L.warps_per_block * sizeof(DensitySmem);
     static LaunchShapeCache cache;
     const int nb = cached_resident_blocks(
-        cache, L, k_density<kPrecise, kBatch, kKern, kNZ, kDense>, threads, sm);
-    k_density<kPrecise, kBatch, kKern, kNZ, kDense><<<nb, threads, sm, L.stream>>>(c, b, ds);
+        cache, L, k_density<kBatch, kKern, kNZ, kDense>, threads, sm);
+    k_density<kBatch, kKern, kNZ, kDense><<<nb, threads, sm, L.stream>>>(c, b, ds);
 }
 
-template <bool kPrecise, bool kBatch, int kKern, bool kNZ = false>
+template <bool kBatch, int kKern, bool kNZ = false>
 static void launch_density_t(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                              DevState* ds) {
-    launch_density_v<kPrecise, kBatch, kKern, kNZ, false>(L, c, b, ds);
-    launch_density_v<kPrecise, kBatch, kKern, kNZ, true>(L, c, b, ds);
+    launch_density_v<kBatch, kKern, kNZ, false>(L, c, b, ds);
+    launch_density_v<kBatch, kKern, kNZ, true>(L, c, b, ds);
 }
 
 template <int kKern>
@@ -215,14 +185,16 @@ static void launch_density_k(const LaunchCtx& L, const StepConst& c, const Buffe
                              DevState* ds) {
     const bool nz = kKern == SPHX_KERNEL_CUBIC_SPLINE && !c.precise && c.div_nz;
     if (b.nscenes > 0) {
-        if (nz) launch_density_t<false, true, kKern, true>(L, c, b, ds);
-        else launch_density_t<false, true, kKern>(L, c, b, ds);
-    } else if (c.precise) launch_density_sweep(L, c, b, ds);
-    else if (nz) launch_density_t<false, false, kKern, true>(L, c, b, ds);
-    else launch_density_t<false, false, kKern>(L, c, b, ds);
+        if (nz) launch_density_t<true, kKern, true>(L, c, b, ds);
+        else launch_density_t<true, kKern>(L, c, b, ds);
+    } else if (nz) launch_density_t<false, kKern, true>(L, c, b, ds);
+    else launch_density_t<false, kKern>(L, c, b, ds);
 }
 
+// Precision mode (single scene) runs the tile sweep (sphx_sweep.cu); exact mode the lean and
+// the dense-chunk variants of k_density.
 int launch_density(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds) {
+    if (c.precise && b.nscenes == 0) return launch_density_sweep(L, c, b, ds);
     if (c.kern == SPHX_KERNEL_WENDLAND_C2) launch_density_k<SPHX_KERNEL_WENDLAND_C2>(L, c, b, ds);
     else if (c.kern == SPHX_KERNEL_GAUSSIAN) launch_density_k<SPHX_KERNEL_GAUSSIAN>(L, c, b, ds);
     else launch_density_k<SPHX_KERNEL_CUBIC_SPLINE>(L, c, b, ds);

@@ -170,49 +170,6 @@ __device__ __forceinline__ void force_term_cubic_x2(const StepConst& c, const fl
     B = make_float2(pz, vz);
 }
 
-// Precision-mode pair term: the pressure and viscosity contributions of candidate j to the
-// force on particle t, summed into one vector (the mode is judged against FP64, not against
-// the reference's summation order), with contracted FP32 arithmetic, the hardware
-// reciprocal square root and exponential, and the candidate's factors of the density
-// pass in aj = (rho, P, m / (2 rho), (m / rho) mu).  Formulas: equations::compute_pressure_force /
-// compute_viscosity_force (sph_engine.cpp:390-432) with grad W = g * r_vec and
-// laplacian W = lap of the kernel; the pressure term is skipped for |r| < 1e-6.
-template <int K>
-__device__ __forceinline__ float3 force_term_fast(const StepConst& c, const float4& xt,
-                                                  const float4& vt, float Pt, const float4& xj,
-                                                  const float4& vj, const float4& aj) {
-    const float dx = xt.x - xj.x, dy = xt.y - xj.y, dz = xt.z - xj.z;
-    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    float r, rinv;
-    fast_len(d2, r, rinv);
-    float g, lap;
-    if (K == SPHX_KERNEL_GAUSSIAN) {
-        const float e = __expf(-d2 * c.gs);
-        g = c.gg * e;
-        lap = c.gl * e * fmaf(c.g2s, d2, -3.0f);
-    } else {
-        const float q = r * c.rcp_h;
-        if (K == SPHX_KERNEL_WENDLAND_C2) {
-            const float t = fmaf(-0.5f, q, 1.0f);
-            const bool in = q < 2.0f;
-            g = in ? c.wnorm * (-5.0f * (t * t * t) * q) * (rinv * c.rcp_h) : 0.0f;
-            lap = in ? c.wl * (t * t) * fmaf(5.0f, q, -3.0f) : 0.0f;
-        } else {
-            const float t = 2.0f - q;
-            const float gf = q <= 1.0f ? c.sigma * q * fmaf(1.5f, q, -2.0f)
-                                       : (q <= 2.0f ? -0.5f * c.sigma * (t * t) : 0.0f);
-            g = gf * (rinv * c.rcp_h);
-            const float sh = c.sigma * c.rcp_hsq;
-            lap = q <= 1.0f ? sh * fmaf(3.0f, q, -2.0f) : (q <= 2.0f ? sh * t : 0.0f);
-        }
-    }
-    if (r < 1e-6f) g = 0.0f;
-    const float cp = -(aj.z * (Pt + aj.y)) * g;  // -(m_j (P_t + P_j) / (2 rho_j)) g
-    const float cv = aj.w * lap;                  // (m_j / rho_j) mu lap
-    return make_float3(fmaf(cp, dx, cv * (vj.x - vt.x)), fmaf(cp, dy, cv * (vj.y - vt.y)),
-                       fmaf(cp, dz, cv * (vj.z - vt.z)));
-}
-
 // Cells holding more particles than this after the grid build mark a collapsed state, in
 // which whole chunks are dense (every particle of a tile within r of every candidate).
 constexpr uint32_t kDenseOccupancy = 128;
@@ -220,9 +177,8 @@ constexpr uint32_t kDenseOccupancy = 128;
 // kDense: the variant with the dense-chunk path (lane-load staging only).  With lane-load
 // staging both variants are launched every step and each returns at once unless the grid's
 // fullest cell says the state is its case.
-template <bool kIntegrate, bool kPrecise, bool kBatch, int kKern, bool kNZ, bool kBulk,
-          bool kDense>
-__global__ void __launch_bounds__(128, kPrecise || kBulk || kDense ? 6 : 7) k_force(
+template <bool kIntegrate, bool kBatch, int kKern, bool kNZ, bool kBulk, bool kDense>
+__global__ void __launch_bounds__(128, kBulk || kDense ? 6 : 7) k_force(
     const StepConst cp, const Buffers b, DevState* ds) {
     if (ds->status) return;
     if (!kBulk && kDense != (ds->max_occ > kDenseOccupancy)) return;
@@ -249,9 +205,7 @@ __global__ void __launch_bounds__(128, kPrecise || kBulk || kDense ? 6 : 7) k_fo
         Tile T;
         float4 xi;
         bool valid;
-        int4 frame = make_int4(0, 0, 0, 0);
-        if (kPrecise) tile_setup_cells(c, b, g, k0, lane, T, xi, valid, frame);
-        else tile_setup(c, b, g, k0, lane, T, xi, valid);
+        tile_setup(c, b, g, k0, lane, T, xi, valid);
         const int i = T.k0 + lane;
         const float4 vi0 = valid ? b.vel4_s[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float Pi = valid ? b.aux4_s[i].y : 0.0f;
@@ -268,7 +222,6 @@ __global__ void __launch_bounds__(128, kPrecise || kBulk || kDense ? 6 : 7) k_fo
         S->tvel[lane] = make_float4(vi0.x, vi0.y, vi0.z, Pi);
         // force sums, packed: pressure (x, y), viscosity (x, y), (pressure z, viscosity z)
         f32x2 fpxy = pk2(0.0f, 0.0f), fvxy = pk2(0.0f, 0.0f), fz = pk2(0.0f, 0.0f);
-        KSum Fx, Fy, Fz;  // precision mode: one compensated sum per component
         const int nseg = build_segments(b, g, T, lane, S->seg);
         __syncwarp();
         // One chunk's work once its candidates are staged (cpos/cvel/caux) and this lane's
@@ -294,18 +247,9 @@ __global__ void __launch_bounds__(128, kPrecise || kBulk || kDense ? 6 : 7) k_fo
             const int lo = max(T.k0, s), hi = min(T.k0 + T.cnt, s + m);
             if (kDense && H == (uint32_t)(T.cnt * m - max(hi - lo, 0))) {
                 const float4 xt = S->tpos[lane], vt = S->tvel[lane];
-                float px = 0.0f, py = 0.0f, pz = 0.0f;
                 float2 sp = upk2(fpxy), sv = upk2(fvxy), sz = upk2(fz);
                 for (int jj = 0; jj < m; ++jj) {
                     if (!valid || jj == self) continue;
-                    if (kPrecise) {
-                        const float3 fv =
-                            force_term_fast<kKern>(c, xt, vt, vt.w, cpos[jj], cvel[jj], caux[jj]);
-                        px += fv.x;
-                        py += fv.y;
-                        pz += fv.z;
-                        continue;
-                    }
                     float4 A;
                     float2 Bv;
                     if (kKern == SPHX_KERNEL_CUBIC_SPLINE) {
@@ -327,16 +271,10 @@ __global__ void __launch_bounds__(128, kPrecise || kBulk || kDense ? 6 : 7) k_fo
                 fpxy = pk2(sp.x, sp.y);
                 fvxy = pk2(sv.x, sv.y);
                 fz = pk2(sz.x, sz.y);
-                if (kPrecise) {
-                    Fx.add(px);
-                    Fy.add(py);
-                    Fz.add(pz);
-                }
                 return;
             }
             list_hits(S->plist, mask, o, lane);
             __syncwarp();
-            float px = 0.0f, py = 0.0f, pz = 0.0f;  // precision mode: this chunk's sums
             for (uint32_t base = 0; base < H; base += kForceBatch) {
                 const uint32_t end = min(H, base + kForceBatch);
                 for (uint32_t f = base + lane; f < end; f += 32) {
@@ -345,20 +283,13 @@ __global__ void __launch_bounds__(128, kPrecise || kBulk || kDense ? 6 : 7) k_fo
                     float p3[3], v3[3];
                     const float4 vt = S->tvel[tt];
                     const uint32_t u = f - base;
-                    if (!kPrecise && kKern == SPHX_KERNEL_CUBIC_SPLINE) {
+                    if (kKern == SPHX_KERNEL_CUBIC_SPLINE) {
                         float4 A;
                         float2 Bp;
                         force_term_cubic_x2<kNZ>(c, S->tpos[tt], vt, vt.w, cpos[jj],
                                             cvel[jj], caux[jj], A, Bp);
                         S->tbA[u] = A;
                         S->tbB[u] = Bp;
-                        continue;
-                    }
-                    if (kPrecise) {
-                        const float3 fv = force_term_fast<kKern>(c, S->tpos[tt], vt, vt.w,
-                                                                 cpos[jj], cvel[jj],
-                                                                 caux[jj]);
-                        S->tbA[u] = make_float4(fv.x, fv.y, fv.z, 0.0f);
                         continue;
                     }
                     force_term<kKern>(c, S->tpos[tt], vt, vt.w, cpos[jj], cvel[jj],
@@ -371,12 +302,6 @@ __global__ void __launch_bounds__(128, kPrecise || kBulk || kDense ? 6 : 7) k_fo
                 for (uint32_t k = max(o, base); k < k1; ++k) {
                     const uint32_t u = k - base;
                     const float4 A = S->tbA[u];
-                    if (kPrecise) {
-                        px += A.x;
-                        py += A.y;
-                        pz += A.z;
-                        continue;
-                    }
                     const float2 Bv = S->tbB[u];
                     // the records hold -(pressure term): three packed additions
                     fpxy = xadd2(fpxy, pk2(A.x, A.y));
@@ -385,19 +310,13 @@ __global__ void __launch_bounds__(128, kPrecise || kBulk || kDense ? 6 : 7) k_fo
                 }
                 __syncwarp();
             }
-            if (kPrecise) {  // compensated across chunks
-                Fx.add(px);
-                Fy.add(py);
-                Fz.add(pz);
-            }
-
         };
         const uint32_t* rec = slot != kNoSlot ? b.hitmask + (size_t)slot * 32 + lane : nullptr;
         const size_t pool_words = (size_t)b.hitmask_cap * 32;
         auto record = [&](const uint32_t* r) -> uint32_t {  // a lane's word, if in the pool
             return r && (size_t)(r - b.hitmask) < pool_words ? __ldcs(r) : 0u;
         };
-        if constexpr (kPrecise || !kBulk) {
+        if constexpr (!kBulk) {
             uint32_t mnext = record(rec);
             for (int sg = 0; sg < nseg; ++sg) {
                 const int2 se = S->seg[sg];
@@ -414,17 +333,14 @@ __global__ void __launch_bounds__(128, kPrecise || kBulk || kDense ? 6 : 7) k_fo
                         const uint32_t used = __reduce_or_sync(kFull, mask);  // candidates hit
                         if (!used) continue;
                         if (used & (1u << lane)) {
-                            float4 pl = b.pos4_s[s + lane];
-                            if (kPrecise) pl = frame_pos(b.cell4_s[s + lane], frame, pl, c.cs);
-                            S->cpos[0][lane] = pl;
+                            S->cpos[0][lane] = b.pos4_s[s + lane];
                             S->cvel[0][lane] = b.vel4_s[s + lane];
                             S->caux[0][lane] = b.aux4_s[s + lane];
                         }
                         __syncwarp();
                     } else {
                         const bool in = lane < m;
-                        float4 pl = in ? b.pos4_s[s + lane] : make_float4(inf, inf, inf, 0.f);
-                        if (kPrecise && in) pl = frame_pos(b.cell4_s[s + lane], frame, pl, c.cs);
+                        const float4 pl = in ? b.pos4_s[s + lane] : make_float4(inf, inf, inf, 0.f);
                         S->cpos[0][lane] = pl;
                         __syncwarp();
                         TileBox B;
@@ -438,7 +354,7 @@ __global__ void __launch_bounds__(128, kPrecise || kBulk || kDense ? 6 : 7) k_fo
                             S->caux[0][lane] = b.aux4_s[s + lane];
                         }
                         __syncwarp();
-                        mask = valid ? chunk_hits<kPrecise>(S->cpos[0], surv, xi, c.r2) : 0u;
+                        mask = valid ? chunk_hits(S->cpos[0], surv, xi, c.r2) : 0u;
                     }
                     process(mask, s, m, S->cpos[0], S->cvel[0], S->caux[0]);
                 }
@@ -504,7 +420,7 @@ __global__ void __launch_bounds__(128, kPrecise || kBulk || kDense ? 6 : 7) k_fo
                         B.hi[0] = hi.x, B.hi[1] = hi.y, B.hi[2] = hi.z;
                         const uint32_t surv =
                             __ballot_sync(kFull, lane < m && box_near(B, cpos[lane], r2m));
-                        mask = valid && surv ? chunk_hits<false>(cpos, surv, xi, c.r2) : 0u;
+                        mask = valid && surv ? chunk_hits(cpos, surv, xi, c.r2) : 0u;
                     }
                     process(mask, s, m, cpos, S->cvel[q], S->caux[q]);
                     __syncwarp();  // buffer q is free once every lane is past this point
@@ -522,39 +438,16 @@ __global__ void __launch_bounds__(128, kPrecise || kBulk || kDense ? 6 : 7) k_fo
         __syncwarp();
         if (!valid) continue;
         const float mi = xi.w;
-        float ax, ay, az;
-        if (kPrecise) {
-            ax = Fx.value() / mi;
-            ay = (Fy.value() + c.grav * mi) / mi;
-            az = Fz.value() / mi;
-        } else {
-            const float2 fp = upk2(fpxy), fv = upk2(fvxy), fzz = upk2(fz);
-            const float fpz = fzz.x, fvz = fzz.y;
-            ax = xdiv(xadd(xadd(fp.x, fv.x), xmul(0.0f, mi)), mi);
-            ay = xdiv(xadd(xadd(fp.y, fv.y), xmul(c.grav, mi)), mi);
-            az = xdiv(xadd(xadd(fpz, fvz), xmul(0.0f, mi)), mi);
-        }
+        const float2 fp = upk2(fpxy), fv = upk2(fvxy), fzz = upk2(fz);
+        const float fpz = fzz.x, fvz = fzz.y;
+        const float ax = xdiv(xadd(xadd(fp.x, fv.x), xmul(0.0f, mi)), mi);
+        const float ay = xdiv(xadd(xadd(fp.y, fv.y), xmul(c.grav, mi)), mi);
+        const float az = xdiv(xadd(xadd(fpz, fvz), xmul(0.0f, mi)), mi);
         b.acc4_s[i] = make_float4(ax, ay, az, 0.0f);
         if (!kIntegrate) continue;
         const float dt = kBatch ? b.scenes[scene].dt : ds->dt;
         const float4 vi = S->tvel[lane];
         const uint32_t id = b.id_s[i];
-        if (kPrecise) {
-            int4 cell = b.cell4_s[i];
-            const float4 own = b.pos4_s[i];
-            float o[3] = {own.x, own.y, own.z}, v[3] = {vi.x, vi.y, vi.z};
-            const float acc[3] = {ax, ay, az};
-            if (!cell.w) integrate_cells(c, dt, acc, o, v, cell);
-            b.cell4[id] = cell;
-            b.pos4[id] = make_float4(o[0], o[1], o[2], mi);
-            b.vel4[id] = make_float4(v[0], v[1], v[2], 0.0f);
-            if (id == 0) {
-                ds->a0[0] = ax;
-                ds->a0[1] = ay;
-                ds->a0[2] = az;
-            }
-            continue;
-        }
         float x[3] = {xi.x, xi.y, xi.z}, v[3] = {vi.x, vi.y, vi.z};
         const float acc[3] = {ax, ay, az};
 #pragma unroll
@@ -588,59 +481,52 @@ __global__ void __launch_bounds__(128, kPrecise || kBulk || kDense ? 6 : 7) k_fo
     }
 }
 
-template <bool kIntegrate, bool kPrecise, bool kBatch, int kKern, bool kNZ, bool kBulk,
-          bool kDense>
+template <bool kIntegrate, bool kBatch, int kKern, bool kNZ, bool kBulk, bool kDense>
 static void launch_force_v(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                            DevState* ds) {
     const int threads = 32 * L.warps_per_block;
     const size_t sm = (size_t)L.warps_per_block * sizeof(ForceSmem<kBulk>);
     static LaunchShapeCache cache;
     const int nb = cached_resident_blocks(
-        cache, L, k_force<kIntegrate, kPrecise, kBatch, kKern, kNZ, kBulk, kDense>, threads, sm);
-    k_force<kIntegrate, kPrecise, kBatch, kKern, kNZ, kBulk, kDense>
+        cache, L, k_force<kIntegrate, kBatch, kKern, kNZ, kBulk, kDense>, threads, sm);
+    k_force<kIntegrate, kBatch, kKern, kNZ, kBulk, kDense>
         <<<nb, threads, sm, L.stream>>>(c, b, ds);
 }
 
-// Exact mode stages candidates by the lanes' own loads or by bulk copies (L.bulk_copy, a
-// tuning choice); precision mode by the lanes' loads (its candidates are converted to the
-// tile's frame as they are staged).  Returns the kernels launched.
-template <bool kIntegrate, bool kPrecise, bool kBatch, int kKern, bool kNZ = false>
+// Candidates are staged by the lanes' own loads or by bulk copies (L.bulk_copy, a tuning
+// choice).  Returns the kernels launched.
+template <bool kIntegrate, bool kBatch, int kKern, bool kNZ = false>
 static int launch_force_t(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                           DevState* ds) {
-    if constexpr (!kPrecise) {
-        if (L.bulk_copy) {
-            launch_force_v<kIntegrate, kPrecise, kBatch, kKern, kNZ, true, false>(L, c, b, ds);
-            return 1;
-        }
+    if (L.bulk_copy) {
+        launch_force_v<kIntegrate, kBatch, kKern, kNZ, true, false>(L, c, b, ds);
+        return 1;
     }
-    launch_force_v<kIntegrate, kPrecise, kBatch, kKern, kNZ, false, false>(L, c, b, ds);
-    launch_force_v<kIntegrate, kPrecise, kBatch, kKern, kNZ, false, true>(L, c, b, ds);
+    launch_force_v<kIntegrate, kBatch, kKern, kNZ, false, false>(L, c, b, ds);
+    launch_force_v<kIntegrate, kBatch, kKern, kNZ, false, true>(L, c, b, ds);
     return 2;
 }
 
 template <int kKern>
 static int launch_force_k(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                           DevState* ds, int integrate) {
-    const bool nz = kKern == SPHX_KERNEL_CUBIC_SPLINE && !c.precise && c.div_nz;
-    if (b.nscenes > 0) {
-        if (integrate) {
-            if (nz) return launch_force_t<true, false, true, kKern, true>(L, c, b, ds);
-            return launch_force_t<true, false, true, kKern>(L, c, b, ds);
-        }
-        return launch_force_t<false, false, true, kKern>(L, c, b, ds);
-    }
+    const bool nz = kKern == SPHX_KERNEL_CUBIC_SPLINE && c.div_nz;
+    const bool batch = b.nscenes > 0;
     if (integrate) {
-        if (c.precise) return launch_force_sweep(L, c, b, ds, 1);
-        if (nz) return launch_force_t<true, false, false, kKern, true>(L, c, b, ds);
-        return launch_force_t<true, false, false, kKern>(L, c, b, ds);
+        if (batch) return nz ? launch_force_t<true, true, kKern, true>(L, c, b, ds)
+                             : launch_force_t<true, true, kKern>(L, c, b, ds);
+        return nz ? launch_force_t<true, false, kKern, true>(L, c, b, ds)
+                  : launch_force_t<true, false, kKern>(L, c, b, ds);
     }
-    if (c.precise) return launch_force_sweep(L, c, b, ds, 0);
-    if (nz) return launch_force_t<false, false, false, kKern, true>(L, c, b, ds);
-    return launch_force_t<false, false, false, kKern>(L, c, b, ds);
+    if (batch) return launch_force_t<false, true, kKern>(L, c, b, ds);
+    return nz ? launch_force_t<false, false, kKern, true>(L, c, b, ds)
+              : launch_force_t<false, false, kKern>(L, c, b, ds);
 }
 
+// Precision mode (single scene) runs the tile sweep (sphx_sweep.cu); exact mode k_force.
 int launch_force(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds,
                  int integrate) {
+    if (c.precise && b.nscenes == 0) return launch_force_sweep(L, c, b, ds, integrate);
     if (c.kern == SPHX_KERNEL_WENDLAND_C2)
         return launch_force_k<SPHX_KERNEL_WENDLAND_C2>(L, c, b, ds, integrate);
     if (c.kern == SPHX_KERNEL_GAUSSIAN)

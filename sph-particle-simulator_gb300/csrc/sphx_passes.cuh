@@ -400,31 +400,21 @@ __device__ __forceinline__ bool box_near(const TileBox& B, const float4& p, floa
     return ex * ex + ey * ey + ez * ez <= r2_margin;
 }
 
-// Hit mask of this lane's particle against the staged chunk (candidates in `surv` only).
-// Exact mode: the reference's rounded test; precision mode: contracted FP32 on
-// frame-relative coordinates.
-template <bool kPrecise>
+// Hit mask of this lane's particle against the staged chunk (candidates in `surv` only):
+// the reference's rounded test.
 __device__ __forceinline__ uint32_t chunk_hits(const float4* cand, uint32_t surv,
                                                const float4& xi, float r2) {
     uint32_t mask = 0;
 #pragma unroll
     for (int jj = 0; jj < 32; ++jj) {
         if (surv & (1u << jj)) {
-            float d2;
-            if (kPrecise) {
-                const float4 xj = cand[jj];
-                const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-                d2 = dx * dx + dy * dy + dz * dz;
-            } else {
-                d2 = diff(xi, cand[jj]).d2;
-            }
-            if (d2 <= r2) mask |= 1u << jj;
+            if (diff(xi, cand[jj]).d2 <= r2) mask |= 1u << jj;
         }
     }
     return mask;
 }
 
-// chunk_hits<false> two candidates at a time with packed FP32 pairs: the same exact test
+// chunk_hits two candidates at a time with packed FP32 pairs: the same exact test
 // (x_i - x_j per axis, (dx*dx + dy*dy) + dz*dz, <= r^2), element by element.  Candidates
 // outside `surv` are farther than r from every lane (the box cull is conservative), so a
 // pair is skipped only when both of its candidates are.
@@ -447,25 +437,8 @@ __device__ __forceinline__ uint32_t chunk_hits_x2(const float* cx, const float* 
     return mask;
 }
 
-// |r| and 1/|r| of a pair from d2 = |r|^2 with the hardware reciprocal square root (a few
-// ulp): precision mode only.  A coincident pair (d2 = 0) gets |r| = 0 and 1/|r| = 0.
-__device__ __forceinline__ void fast_len(float d2, float& r, float& rinv) {
-    rinv = d2 > 0.0f ? rsqrtf(d2) : 0.0f;
-    r = d2 * rinv;
-}
-
-// W(q) in precision mode: the same formula with contracted arithmetic, both branches
-// evaluated and one selected (q of a hit is at most 2 up to rounding)
-__device__ __forceinline__ float cubic_w_fast(const StepConst& c, float q) {
-    const float t = 2.0f - q;
-    const float w1 = c.sigma * fmaf(q * q, fmaf(0.5f, q, -1.0f), 2.0f / 3.0f);
-    const float w2 = c.sigma * (1.0f / 6.0f) * (t * t * t);
-    return q <= 1.0f ? w1 : (q <= 2.0f ? w2 : 0.0f);
-}
-
-// W of the pair (x_i - x_j = (dx, dy, dz), d2 = |.|^2) for smoothing kernel K.
-// Exact mode: the reference's float operations (Kernel::W, kernels.cpp:140-143, 172-178,
-// 210-213); precision mode: contracted arithmetic.
+// W of the pair (x_i - x_j = (dx, dy, dz), d2 = |.|^2) for smoothing kernel K, with the
+// reference's float operations (Kernel::W, kernels.cpp:140-143, 172-178, 210-213).
 // kNZ: d2 <= r^2 (a hit), so |r| is +0 or in [2^-74.5, r (1 + 2^-23)], which the host
 // keeps inside xdiv_fixed_nz's range
 template <int K, bool kNZ = false>
@@ -474,21 +447,6 @@ __device__ __forceinline__ float pair_w_exact(const StepConst& c, float d2) {
     const float q = kNZ ? xdiv_fixed_nz(xsqrt(d2), c.h, c.rcp_h)
                         : xdiv_fixed(xsqrt(d2), c.h, c.rcp_h, c.fast_div_h);
     return K == SPHX_KERNEL_WENDLAND_C2 ? wendland_w(c, q) : cubic_w(c, q);
-}
-// W of a pair in precision mode: contracted arithmetic, hardware reciprocal square root
-// and exponential (errors of a few ulp per term, far inside the stated bounds)
-template <int K>
-__device__ __forceinline__ float pair_w_fast(const StepConst& c, float d2) {
-    if (K == SPHX_KERNEL_GAUSSIAN) return c.wnorm * __expf(-d2 * c.gs);
-    float r, rinv;
-    fast_len(d2, r, rinv);
-    const float q = r * c.rcp_h;
-    if (K == SPHX_KERNEL_WENDLAND_C2) {
-        const float t = fmaf(-0.5f, q, 1.0f);
-        const float t2 = t * t;
-        return q < 2.0f ? c.wnorm * (t2 * t2) * fmaf(2.0f, q, 1.0f) : 0.0f;
-    }
-    return cubic_w_fast(c, q);
 }
 
 // Precision-mode leapfrog + wall clamp on cell + offset positions (FP64 clamp).
