@@ -62,6 +62,20 @@ METRIC = "particle-steps/s at 1M and 10M (+% HBM roofline); batched vs plain at 
 UNIT = "particle-steps/s"
 FORCE_BYTES_PER_PARTICLE = 72    # read x,v,rho,P,m (36 B); write x,v,a (36 B)
 DENSITY_BYTES_PER_PARTICLE = 24  # read x,m (16 B); write rho,P (8 B)
+# The passes of each mode: the kernels measured, their algorithmic bytes per particle and
+# the keys of their committed ncu summaries.  Precision mode stores a position as an
+# integer cell (12 B) plus an FP32 offset (12 B): force reads x (24), v, rho, P, m (24) and
+# writes x, v, a (48); density reads x, m (28) and writes rho, P (8).
+PASSES = {
+    "exact": {"force": "k_force<1,0,0,0,1,0,0> (force + leapfrog + clamp)",
+              "density": "k_density<0,0,0,1,0>", "force_bytes": FORCE_BYTES_PER_PARTICLE,
+              "density_bytes": DENSITY_BYTES_PER_PARTICLE, "issue_force": "k_force",
+              "issue_density": "k_density", "traffic": "force"},
+    "precise": {"force": "k_force_sweep<1,0,0> (force + leapfrog + clamp, tile sweep)",
+                "density": "k_density_sweep<0>", "force_bytes": 96, "density_bytes": 36,
+                "issue_force": "k_force_sweep", "issue_density": "k_density_sweep",
+                "traffic": "force_sweep"},
+}
 # published CPU figure for the 1M case: README.md:45, 38 steps/s at 1M particles
 PUBLISHED_1M = 38.0 * 1_000_000
 L2_FLUSH_BYTES = 512 << 20
@@ -102,17 +116,18 @@ def peaks() -> tuple[float, str]:
     return FALLBACK_HBM_GBS, "fallback"
 
 
-def ncu_traffic(workload_name: str, n: int):
-    """Per-launch DRAM bytes of the force kernel from the committed ncu summary (measured
-    per particle on the 4.1M lattice, whose arrays exceed L2), scaled to this workload's
-    particle count; returns (total, hit-mask records part) or (None, None)."""
+def ncu_traffic(key: str, n: int):
+    """Per-launch DRAM bytes of a force kernel ("force": exact mode, "force_sweep":
+    precision mode) from the committed ncu summary (measured per particle on the 4.1M
+    lattice, whose arrays exceed L2), scaled to this workload's particle count; returns
+    (total, hit-mask records part) or (None, None)."""
     p = REPO / "profiles" / "ncu_traffic.json"
     if not p.exists():
         return None, None
     try:
-        d = json.loads(p.read_text())
-        f = d["force"]
-        return float(f["dram_bytes_per_particle"]) * n, float(f["hit_mask_bytes_per_particle"]) * n
+        f = json.loads(p.read_text())[key]
+        return (float(f["dram_bytes_per_particle"]) * n,
+                float(f.get("hit_mask_bytes_per_particle", 0.0)) * n)
     except Exception:
         return None, None
 
@@ -503,10 +518,29 @@ def bench_10m_precise(torch, stream, flush, w10, steps):
     st = ctx.stats()
     t, dt = ctx.time_f64()
     ctx.close()
+    # the kernel split, from an eager context with phase timers (same state, same steps)
+    pc = sphx.Context(w10.n, mode=sphx.MODE_PRECISE, profile=True)
+    pc.set_stream(stream.cuda_stream)
+    pc.set_params(w10.params)
+    pc.upload(w10.pos, w10.vel, w10.mass)
+    pc.snapshot()
+    pc.restore()
+    pc.step(0.0)
+    torch.cuda.synchronize()
+    pc.reset_stats()
+    timed_steps(torch, pc, w10, 3, flush)
+    ps = pc.stats()
+    pc.close()
+    f10 = ps["force_computation_time"] / 3
     return {"value": w10.n * steps / (sum(ms) * 1e-3), "unit": UNIT, "steps": steps,
             "ms_per_step": sum(ms) / steps, "mode": "cell + FP32 offset, compensated sums",
             "last_dt_s": dt, "fp64_sum_mass": st["sum_mass"],
             "fp64_energy": st["kinetic_energy"] + st["potential_energy"],
+            "force_kernel_ms": 1e3 * f10,
+            "density_kernel_ms": 1e3 * ps["density_computation_time"] / 3,
+            "grid_build_ms": 1e3 * ps["neighbor_search_time"] / 3,
+            "force_hbm_frac": (PASSES["precise"]["force_bytes"] * w10.n / f10 / 1e9) / peaks()[0],
+            "kernels": [PASSES["precise"]["density"], PASSES["precise"]["force"]],
             "protocol": "fresh-state, CFL dt in FP64 (step(0)), captured graph"}
 
 
@@ -700,25 +734,26 @@ def bench_ours(args, world, rank, local):
         return 0
 
     peak, peak_kind = peaks()
-    achieved = FORCE_BYTES_PER_PARTICLE * w.n / force_s / 1e9
+    ps = PASSES[args.mode]
+    achieved = ps["force_bytes"] * w.n / force_s / 1e9
     # the bound that applies: instruction issue (the passes do ~8 FP32 ops per candidate
     # test and ~150 per exact pair term on L1/L2-resident data)
     sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
     sms = torch.cuda.get_device_properties(local).multi_processor_count or SM_COUNT_FALLBACK
     issue_peak = sms * ISSUE_PER_SM_PER_CLK * sm_mhz * 1e6
     issue = None
-    ipp = ncu_issue("k_force")
+    ipp = ncu_issue(ps["issue_force"])
     if ipp:
         a_issue = ipp * w.n / force_s
         issue = {"bound": "issue", "achieved": a_issue, "peak": issue_peak,
                  "unit": "warp-inst/s", "frac": a_issue / issue_peak,
-                 "kernel": "k_force<true>",
+                 "kernel": ps["force"],
                  "source": "profiles/ncu_issue.json warp instructions per particle x particles "
                            "/ CUDA-event kernel time; peak = SMs x 4 issue slots x median SM clock"}
-        ipd = ncu_issue("k_density")
+        ipd = ncu_issue(ps["issue_density"])
         if ipd:
             issue["density_frac"] = ipd * w.n / dens_s / issue_peak
-    traffic, traffic_masks = ncu_traffic(args.workload, w.n)
+    traffic, traffic_masks = ncu_traffic(ps["traffic"], w.n)
     cpu = None
     if world == 1 and not args.no_cpu:
         cpu = run_cpu(w, steps=8, warmup=0, budget_s=15.0)
@@ -742,17 +777,21 @@ def bench_ours(args, world, rank, local):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "traffic_hit_masks": traffic_masks,
-                     "traffic_note": "DRAM bytes per launch = the particle data (%.1fx the "
-                                     "72 B/particle algorithmic bytes) + the hit-mask records "
-                                     "the density pass wrote for this pass (read once)"
-                                     % ((traffic - traffic_masks) / (72.0 * w.n)
-                                        if traffic and traffic_masks else float("nan")),
-                     "kernel": "k_force<true> (force + leapfrog + clamp)",
+                     "traffic_note": ("DRAM bytes per launch = the particle data (%.1fx the "
+                                      "%d B/particle algorithmic bytes) + the hit-mask records "
+                                      "the density pass wrote for this pass (read once)"
+                                      % ((traffic - traffic_masks) / (ps["force_bytes"] * w.n),
+                                         ps["force_bytes"])) if traffic and traffic_masks else
+                                     ("DRAM bytes per launch = %.1fx the %d B/particle "
+                                      "algorithmic bytes (no hit-mask records in this mode)"
+                                      % (traffic / (ps["force_bytes"] * w.n), ps["force_bytes"])
+                                      if traffic else None),
+                     "kernel": ps["force"],
                      "peak_source": f"{peak_kind} hbm_gbs"},
         "roofline_issue": issue,
         "kernels_ms": {"grid_build": 1e3 * grid_s, "density": 1e3 * dens_s,
-                       "force": 1e3 * force_s,
-                       "density_hbm_frac": (DENSITY_BYTES_PER_PARTICLE * w.n / dens_s / 1e9) / peak},
+                       "force": 1e3 * force_s, "density_kernel": ps["density"],
+                       "density_hbm_frac": (ps["density_bytes"] * w.n / dens_s / 1e9) / peak},
         "gpu_launches": launches,
         "clocks": clocks,
         "cpu_baseline": cpu and {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
