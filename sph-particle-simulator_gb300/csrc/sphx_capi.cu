@@ -646,22 +646,25 @@ int sphx_create(sphx_ctx** out, size_t capacity, const sphx_tuning* tuning) {
     if (c->tuning.mode != SPHX_MODE_EXACT &&
         ((rc = dmalloc(&b.cell4, C)) || (rc = dmalloc(&b.cell4_s, C))))
         return fail(rc);
-    // Hit-mask pool: 4 records (128 B each) per particle of capacity.  A dense state needs
-    // about 1.7-2.6 per particle (32-particle tiles, 27-cell stencil); the rest is slack for
-    // the uneven split of tiles over the warps.  Without the pool (or where a warp's region
-    // runs out) the force pass repeats the distance tests.
-    if (dmalloc(&b.tile_slot, C) == SPHX_OK) {
-        unsigned long long cap = 4ull * C;
-        if (cap > 0xffff0000ull) cap = 0xffff0000ull;  // record indices are 32-bit
-        if (dmalloc(&b.hitmask, (size_t)cap * 32) == SPHX_OK) {
-            b.hitmask_cap = cap;
+    // Hit-mask pool (exact mode; the precision mode's sweeps keep no records): 4 records
+    // (128 B each) per particle of capacity.  A dense state needs about 1.7-2.6 per particle
+    // (32-particle tiles, 27-cell stencil); the rest is slack for the uneven split of tiles
+    // over the warps.  Without the pool (or where a warp's region runs out) the force pass
+    // repeats the distance tests.
+    if (c->tuning.mode == SPHX_MODE_EXACT) {
+        if (dmalloc(&b.tile_slot, C) == SPHX_OK) {
+            unsigned long long cap = 4ull * C;
+            if (cap > 0xffff0000ull) cap = 0xffff0000ull;  // record indices are 32-bit
+            if (dmalloc(&b.hitmask, (size_t)cap * 32) == SPHX_OK) {
+                b.hitmask_cap = cap;
+            } else {
+                cudaGetLastError();
+                cudaFree(b.tile_slot);
+                b.tile_slot = nullptr;
+            }
         } else {
             cudaGetLastError();
-            cudaFree(b.tile_slot);
-            b.tile_slot = nullptr;
         }
-    } else {
-        cudaGetLastError();
     }
     if (cudaMemset(c->ds, 0, sizeof(DevState)) != cudaSuccess) return fail(SPHX_ERR_CUDA);
     if (cudaHostAlloc(reinterpret_cast<void**>(&c->h_status), sizeof(int), cudaHostAllocDefault) !=

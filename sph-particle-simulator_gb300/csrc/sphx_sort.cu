@@ -270,7 +270,8 @@ struct TileSrc {
         return (k - st) % tile_n == 0 ? 1u : 0u;
     }
 };
-// Writes the tile starts and counts the occupied cells and the fullest one.
+// Writes the tile starts and counts the occupied cells and the fullest one (the threads
+// of a warp call it together: one atomic of each kind per warp and call).
 struct TileSink {
     const uint32_t* key_s;
     const uint32_t* off;
@@ -279,9 +280,14 @@ struct TileSink {
     __device__ void operator()(uint32_t k, uint32_t excl, uint32_t v) const {
         if (v) tile_start[excl] = k;
         const uint32_t c = key_s[k];
-        if (c < ds->ncells && off[c] == k) {
-            atomicAdd(&ds->occupied, 1u);
-            atomicMax(&ds->max_occ, off[c + 1] - k);
+        const bool start = c < ds->ncells && off[c] == k;
+        const unsigned am = __activemask();
+        const unsigned starts = __ballot_sync(am, start);
+        if (!starts) return;
+        const uint32_t occ = __reduce_max_sync(am, start ? off[c + 1] - k : 0u);
+        if ((threadIdx.x & 31) == (uint32_t)(__ffs(am) - 1)) {
+            atomicAdd(&ds->occupied, (uint32_t)__popc(starts));
+            atomicMax(&ds->max_occ, occ);
         }
     }
 };
