@@ -19,8 +19,8 @@
 //
 // Smoothing kernels in the "max form" (a = max(2 - q, 0), b = max(1 - q, 0) for the cubic
 // spline), which is zero beyond the support without a test:
-//   cubic spline  W = sigma/6 (a^3 - 4 b^3),  dW/dq = sigma/2 (4 b^2 - a^2),
-//                 d2W/dq2 = sigma (a - 4 b)          (kernels.cpp:23-60, piecewise there)
+//   cubic spline  dW/dq = sigma/2 (4 b^2 - a^2), d2W/dq2 = sigma (a - 4 b) (kernels.cpp:23-60,
+//                 piecewise there); W itself keeps the piecewise form (sweep_w)
 //   Wendland C2   t = max(1 - q/2, 0):  W = norm t^4 (1 + 2 q), dW/dq = -5 norm t^3 q,
 //                 laplacian = norm (5/h^2) t^2 (5 q - 3)      (kernels.cpp:172-200)
 //   Gaussian      no compact support: every term is masked by the neighbour test
@@ -79,6 +79,7 @@ constexpr float kFar = 1.0e15f;
 // The sweeps' lengths in units of h.
 struct SweepUnits {
     float inv;   // 1/h: metres -> sweep units
+    float cs;    // the cell size in sweep units
     float r2;    // r_search^2 / h^2: the neighbour test
     float r2m;   // the same with the box cull's margin
     float skip2; // (1e-6 m / h)^2: the Gaussian's pressure-term skip
@@ -86,17 +87,26 @@ struct SweepUnits {
 __device__ __forceinline__ SweepUnits sweep_units(const StepConst& c) {
     SweepUnits u;
     u.inv = c.rcp_h;
+    u.cs = c.cs * c.rcp_h;  // 2 exactly for r_search = 2h
     u.r2 = c.r2 * c.rcp_hsq;
     u.r2m = u.r2 * 1.0001f;
     u.skip2 = 1e-12f * c.rcp_hsq;
     return u;
 }
-__device__ __forceinline__ float4 scaled(const float4& x, float inv) {
-    return make_float4(x.x * inv, x.y * inv, x.z * inv, x.w);
+// A particle (cell, offset o, mass in o.w) in the tile's frame, in sweep units: the cell
+// difference times the cell size plus the offset scaled, one rounding each (as frame_pos
+// does in metres).
+__device__ __forceinline__ float4 frame_pos_h(const int4& cell, const int4& frame,
+                                              const float4& o, const SweepUnits& U) {
+    return make_float4(fmaf((float)(cell.x - frame.x), U.cs, o.x * U.inv),
+                       fmaf((float)(cell.y - frame.y), U.cs, o.y * U.inv),
+                       fmaf((float)(cell.z - frame.z), U.cs, o.z * U.inv), o.w);
 }
 
 // W of two pairs (d2 = (|r|/h)^2 of each) up to the kernel's constant factor
-// (sweep_w_scale); the Gaussian's exp(-|r|^2 / h^2) is exp(-d2).
+// (sweep_w_scale); the Gaussian's exp(-|r|^2 / h^2) is exp(-d2).  The cubic spline is the
+// reference's piecewise polynomial (2/3 - q^2 + q^3/2 on [0, 1], (2 - q)^3 / 6 beyond, with
+// 2 - q clamped at 0), selected per pair: no cancellation at small q.
 template <int K>
 __device__ __forceinline__ F2 sweep_w(const StepConst& c, F2 d2) {
     const float2 e = upk2(d2.v);
@@ -107,11 +117,14 @@ __device__ __forceinline__ F2 sweep_w(const StepConst& c, F2 d2) {
         const F2 t2 = t * t;
         return (t2 * t2) * fma2(q, f2(2.0f), f2(1.0f));
     }
-    const F2 a = max0(f2(2.0f) - q), b = max0(f2(1.0f) - q);
-    return fma2((b * b) * b, f2(-4.0f), (a * a) * a);
+    const F2 w1 = fma2(q * q, fma2(q, f2(0.5f), f2(-1.0f)), f2(2.0f / 3.0f));
+    const F2 t = max0(f2(2.0f) - q);
+    const F2 w2 = (t * t) * (t * f2(1.0f / 6.0f));
+    const float2 qv = upk2(q.v), a = upk2(w1.v), bb = upk2(w2.v);
+    return f2(qv.x <= 1.0f ? a.x : bb.x, qv.y <= 1.0f ? a.y : bb.y);
 }
 __host__ __device__ __forceinline__ float sweep_w_scale(const StepConst& c) {
-    return c.kern == SPHX_KERNEL_CUBIC_SPLINE ? c.sigma * (1.0f / 6.0f) : c.wnorm;
+    return c.kern == SPHX_KERNEL_CUBIC_SPLINE ? c.sigma : c.wnorm;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -142,7 +155,7 @@ __global__ void __launch_bounds__(128, 7) k_density_sweep(const StepConst c, con
         int4 frame;
         tile_setup_cells(c, b, g, b.tile_start[t], lane, T, xi, valid, frame);
         const int i = T.k0 + lane;
-        xi = scaled(xi, U.inv);
+        if (valid && T.cells) xi = frame_pos_h(b.cell4_s[i], frame, b.pos4_s[i], U);
         {
             const TileBox B = tile_box(xi, valid);
             if (lane == 0) {
@@ -160,7 +173,7 @@ __global__ void __launch_bounds__(128, 7) k_density_sweep(const StepConst c, con
             for (int s = se.x; s < se.y; s += 32) {
                 const bool in = lane < se.y - s;
                 float4 pl = make_float4(kFar, kFar, kFar, 0.0f);
-                if (in) pl = scaled(frame_pos(b.cell4_s[s + lane], frame, b.pos4_s[s + lane], c.cs), U.inv);
+                if (in) pl = frame_pos_h(b.cell4_s[s + lane], frame, b.pos4_s[s + lane], U);
                 TileBox B;
                 {
                     const float4 lo = S->box_lo, hi = S->box_hi;
@@ -319,7 +332,7 @@ __global__ void __launch_bounds__(128, 6) k_force_sweep(const StepConst c, const
         int4 frame;
         tile_setup_cells(c, b, g, b.tile_start[t], lane, T, xi, valid, frame);
         const int i = T.k0 + lane;
-        xi = scaled(xi, U.inv);
+        if (valid && T.cells) xi = frame_pos_h(b.cell4_s[i], frame, b.pos4_s[i], U);
         {
             const TileBox B = tile_box(xi, valid);
             if (lane == 0) {
@@ -342,7 +355,7 @@ __global__ void __launch_bounds__(128, 6) k_force_sweep(const StepConst c, const
             for (int s = se.x; s < se.y; s += 32) {
                 const bool in = lane < se.y - s;
                 float4 pl = make_float4(kFar, kFar, kFar, 0.0f);
-                if (in) pl = scaled(frame_pos(b.cell4_s[s + lane], frame, b.pos4_s[s + lane], c.cs), U.inv);
+                if (in) pl = frame_pos_h(b.cell4_s[s + lane], frame, b.pos4_s[s + lane], U);
                 TileBox B;
                 {
                     const float4 lo = S->box_lo, hi = S->box_hi;
