@@ -121,16 +121,33 @@ class SPHEngine {
     // (3), kinetic energy, potential energy (-m g y), sum of densities.
     std::vector<double> get_conservation_sums() const;
 
+    // Copies of the current state into caller arrays, read from the device without
+    // refreshing the whole host mirror (what get_positions & co. return, without the
+    // intermediate vector): positions / velocities 3 floats per particle (particle_count()
+    // particles), densities / pressures the capacity-length arrays of get_densities /
+    // get_pressures.  Not in the reference's API; the Python module's getters use them.
+    size_t particle_count() const { return particles_.size(); }
+    size_t density_count() const { return densities_.size(); }
+    void copy_positions(float* out) const;
+    void copy_velocities(float* out) const;
+    void copy_densities(float* out) const;
+    void copy_pressures(float* out) const;
+
    private:
     void push_params();
     void sync_to_host() const;   // device -> host mirror, when the device is newer
     void sync_to_device();       // host mirror -> device, when the host changed
     void host_will_change();     // call before mutating the host mirror
+    void replace_particles(const std::vector<Particle>& ps);
+    void stage_append(size_t from);  // mirror particles [from, size) -> upload region
+    void copy_field(int field, float* out) const;
 
     float* stage() const;        // pinned transfer buffers (15 floats per particle)
 
     mutable ParticleSystem particles_;
-    mutable float* stage_ = nullptr;   // x, v, m (upload) | x, v, rho, P (download)
+    mutable float* stage_ = nullptr;   // x, v, m (upload) | rho, P, x, v (download)
+    size_t staged_ = 0;                // particles the upload region holds
+    bool stage_current_ = false;       // the upload region equals the mirror's first staged_
     SPHParameters params_;
     KernelType kernel_type_ = KernelType::CUBIC_SPLINE;
     sphx_ctx* gpu_ = nullptr;

@@ -55,12 +55,17 @@ SPHEngine::~SPHEngine() {
     sphx_free_host(stage_);
 }
 
-// Page-locked transfer buffers sized for the capacity, made on first use: 7 floats per
-// particle for the upload (x, v, m: read in place by the GPU when the stream reaches the
-// upload, so they are written only after the stream went idle -- every path that changes
-// the host set downloads, and so synchronises, first) and 8 for the download (x, v, rho,
-// P).  Null when page-locked memory is not available: the transfers then go through
+// Page-locked transfer buffers sized for the capacity C, made on first use, 15 floats per
+// particle: the upload region x [0, 3C), v [3C, 6C), m [6C, 7C) -- read in place by the GPU
+// when the stream reaches the upload, so written only after the stream went idle (every
+// path that changes the host set downloads, and so synchronises, first) -- and the
+// download region rho [7C, 8C), P [8C, 9C), x [9C, 12C), v [12C, 15C) for the single-field
+// copies.  Null when page-locked memory is not available: the transfers then go through
 // ordinary vectors.
+//
+// The upload region is kept equal to the mirror (`stage_current_`, first `staged_`
+// particles): a download writes the device's x and v straight into it, an addition
+// appends its particles, a clear empties it; step() then uploads it as it is.
 float* SPHEngine::stage() const {
     if (!stage_) {
         void* p = nullptr;
@@ -93,39 +98,74 @@ void SPHEngine::initialize_dam_break() {
     if (!initialized_) initialize(SPHParameters{});
     auto ps = utils::create_dam_break_setup(glm::vec3(0.4f, 0.6f, 0.8f),
                                             glm::vec3(0.2f, 0.4f, 0.8f), 0.01f, params_);
-    host_will_change();
-    particles_.clear();
-    particles_.add_particles(ps);
+    replace_particles(ps);
 }
 
 void SPHEngine::initialize_fluid_drop() {
     if (!initialized_) initialize(SPHParameters{});
     auto ps = utils::create_fluid_drop_setup(glm::vec3(0.0f, 0.5f, 0.0f), 0.1f, 0.008f, params_);
-    host_will_change();
-    particles_.clear();
-    particles_.add_particles(ps);
+    replace_particles(ps);
 }
 
 void SPHEngine::initialize_granular_flow() {
     if (!initialized_) initialize(SPHParameters{});
     auto ps = utils::create_granular_flow_setup(glm::vec3(0.3f, 0.4f, 0.8f),
                                                 glm::vec3(1.0f, 1.0f, 1.0f), 0.012f, params_);
+    replace_particles(ps);
+}
+
+// the initialize_* scenes: the host set replaced by `ps`
+void SPHEngine::replace_particles(const std::vector<Particle>& ps) {
     host_will_change();
     particles_.clear();
+    staged_ = 0;
     particles_.add_particles(ps);
+    stage_append(0);
 }
 
 void SPHEngine::add_particles(const std::vector<Particle>& particles) {
     host_will_change();
+    const size_t old = particles_.size();
     particles_.add_particles(particles);
+    stage_append(old);
 }
 
 // SPHEngine::clear_particles (src/sph_engine.cpp:87-91)
 void SPHEngine::clear_particles() {
     host_will_change();
     particles_.clear();
+    staged_ = 0;
     step_count_ = 0;
     check(sphx_set_time(gpu_, 0.0f), "sphx_set_time");
+}
+
+// The mirror's particles [from, size()) appended to the upload region; the region stays
+// current only if it held the first `from` of them.
+void SPHEngine::stage_append(size_t from) {
+    float* buf = stage();
+    const size_t n = particles_.size();
+    if (!buf || staged_ != from) {
+        stage_current_ = false;
+        return;
+    }
+    const size_t C = std::max<size_t>(particles_.capacity(), 1);
+    float* x = buf;
+    float* v = buf + 3 * C;
+    float* m = buf + 6 * C;
+    const long long a = static_cast<long long>(from), e = static_cast<long long>(n);
+#pragma omp parallel for schedule(static) if (e - a > 65536)
+    for (long long i = a; i < e; ++i) {
+        const Particle& p = particles_[static_cast<size_t>(i)];
+        x[3 * i] = p.position.x;
+        x[3 * i + 1] = p.position.y;
+        x[3 * i + 2] = p.position.z;
+        v[3 * i] = p.velocity.x;
+        v[3 * i + 1] = p.velocity.y;
+        v[3 * i + 2] = p.velocity.z;
+        m[i] = p.mass;
+    }
+    staged_ = n;
+    stage_current_ = true;
 }
 
 void SPHEngine::host_will_change() {
@@ -136,15 +176,19 @@ void SPHEngine::host_will_change() {
 void SPHEngine::sync_to_device() {
     if (!device_dirty_) return;
     const size_t n = particles_.size();
-    std::vector<float> fallback;
     float* buf = stage();
-    if (!buf) {
-        fallback.resize(7 * std::max<size_t>(n, 1));
-        buf = fallback.data();
+    if (buf && !(stage_current_ && staged_ == n)) {  // rebuild the upload region
+        staged_ = 0;
+        stage_current_ = true;
+        stage_append(0);
     }
-    float* x = buf;
-    float* v = buf + 3 * n;
-    float* m = buf + 6 * n;
+    if (buf) {
+        const size_t C = std::max<size_t>(particles_.capacity(), 1);
+        check(sphx_upload(gpu_, n, buf, buf + 3 * C, buf + 6 * C), "sphx_upload");
+        device_dirty_ = false;
+        return;
+    }
+    std::vector<float> x(3 * std::max<size_t>(n, 1)), v(x.size()), m(std::max<size_t>(n, 1));
     const long long nn = static_cast<long long>(n);
 #pragma omp parallel for schedule(static) if (nn > 65536)
     for (long long i = 0; i < nn; ++i) {
@@ -157,28 +201,33 @@ void SPHEngine::sync_to_device() {
         v[3 * i + 2] = p.velocity.z;
         m[i] = p.mass;
     }
-    check(sphx_upload(gpu_, n, x, v, m), "sphx_upload");
+    check(sphx_upload(gpu_, n, x.data(), v.data(), m.data()), "sphx_upload");
     device_dirty_ = false;
 }
 
 // Device -> host mirror: positions, velocities, densities and pressures of the last step
 // (particle.density / particle.pressure are written like compute_densities /
-// compute_pressures do, cpp:203-224; particle.acceleration is left as it is).
+// compute_pressures do, cpp:203-224; particle.acceleration is left as it is).  x and v
+// arrive in the upload region, which then equals the mirror again.
 void SPHEngine::sync_to_host() const {
     if (!host_stale_) return;
     const size_t n = particles_.size();
+    const size_t C = std::max<size_t>(particles_.capacity(), 1);
     std::vector<float> fallback;
     float* buf = stage();
+    float *x, *v, *rho, *P;
     if (buf) {
-        buf += 7 * std::max<size_t>(particles_.capacity(), 1);  // the download region
+        x = buf;
+        v = buf + 3 * C;
+        rho = buf + 7 * C;
+        P = buf + 8 * C;
     } else {
         fallback.resize(8 * std::max<size_t>(n, 1));
-        buf = fallback.data();
+        x = fallback.data();
+        v = x + 3 * n;
+        rho = x + 6 * n;
+        P = x + 7 * n;
     }
-    float* x = buf;
-    float* v = buf + 3 * n;
-    float* rho = buf + 6 * n;
-    float* P = buf + 7 * n;
     check(sphx_download(gpu_, x, v, rho, P, nullptr), "sphx_download");
     const long long nn = static_cast<long long>(n);
     const size_t nd = densities_.size(), np = pressures_.size();
@@ -193,6 +242,57 @@ void SPHEngine::sync_to_host() const {
         if (static_cast<size_t>(i) < np) pressures_[i] = P[i];
     }
     host_stale_ = false;
+}
+
+// One field of the current state into out (3 or 1 floats per particle), from the device
+// when it holds a newer state than the mirror (the mirror is left as it is), else from the
+// mirror.  field: 0 x, 1 v, 2 rho, 3 P.
+void SPHEngine::copy_field(int field, float* out) const {
+    const size_t n = particles_.size();
+    if (n == 0) return;
+    const long long nn = static_cast<long long>(n);
+    const int w = field < 2 ? 3 : 1;
+    if (!host_stale_) {
+#pragma omp parallel for schedule(static) if (nn > 65536)
+        for (long long i = 0; i < nn; ++i) {
+            const Particle& p = particles_[static_cast<size_t>(i)];
+            if (field == 0 || field == 1) {
+                const glm::vec3& q = field == 0 ? p.position : p.velocity;
+                out[3 * i] = q.x;
+                out[3 * i + 1] = q.y;
+                out[3 * i + 2] = q.z;
+            } else {
+                out[i] = field == 2 ? p.density : p.pressure;
+            }
+        }
+        return;
+    }
+    float* buf = stage();
+    const size_t C = std::max<size_t>(particles_.capacity(), 1);
+    float* tmp = buf ? buf + (field == 0 ? 9 * C : field == 1 ? 12 * C : field == 2 ? 7 * C : 8 * C)
+                     : out;
+    check(sphx_download(gpu_, field == 0 ? tmp : nullptr, field == 1 ? tmp : nullptr,
+                        field == 2 ? tmp : nullptr, field == 3 ? tmp : nullptr, nullptr),
+          "sphx_download");
+    if (tmp == out) return;
+    const long long words = nn * w;
+#pragma omp parallel for schedule(static) if (words > 65536)
+    for (long long i = 0; i < words; ++i) out[i] = tmp[i];
+}
+
+void SPHEngine::copy_positions(float* out) const { copy_field(0, out); }
+void SPHEngine::copy_velocities(float* out) const { copy_field(1, out); }
+
+// densities / pressures: the capacity-length vectors get_densities / get_pressures return
+void SPHEngine::copy_densities(float* out) const {
+    const size_t n = std::min(particles_.size(), densities_.size());
+    std::copy(densities_.begin() + static_cast<std::ptrdiff_t>(n), densities_.end(), out + n);
+    if (n) copy_field(2, out);
+}
+void SPHEngine::copy_pressures(float* out) const {
+    const size_t n = std::min(particles_.size(), pressures_.size());
+    std::copy(pressures_.begin() + static_cast<std::ptrdiff_t>(n), pressures_.end(), out + n);
+    if (n) copy_field(3, out);
 }
 
 // SPHEngine::step (src/sph_engine.cpp:93-144)
@@ -311,23 +411,27 @@ float SPHEngine::get_total_energy() const {
 }
 
 std::vector<glm::vec3> SPHEngine::get_positions() const {
-    sync_to_host();
-    return particles_.get_positions();
+    std::vector<glm::vec3> out(particles_.size());
+    if (!out.empty()) copy_positions(&out[0].x);
+    return out;
 }
 
 std::vector<glm::vec3> SPHEngine::get_velocities() const {
-    sync_to_host();
-    return particles_.get_velocities();
+    std::vector<glm::vec3> out(particles_.size());
+    if (!out.empty()) copy_velocities(&out[0].x);
+    return out;
 }
 
 std::vector<float> SPHEngine::get_densities() const {
-    sync_to_host();
-    return densities_;
+    std::vector<float> out(densities_.size());
+    if (!out.empty()) copy_densities(out.data());
+    return out;
 }
 
 std::vector<float> SPHEngine::get_pressures() const {
-    sync_to_host();
-    return pressures_;
+    std::vector<float> out(pressures_.size());
+    if (!out.empty()) copy_pressures(out.data());
+    return out;
 }
 
 std::vector<double> SPHEngine::get_conservation_sums() const {

@@ -216,10 +216,27 @@ PYBIND11_MODULE(sph, m) {
         .def("get_conservation_sums", &sph::SPHEngine::get_conservation_sums)
         .def("validate_simulation", &sph::SPHEngine::validate_simulation)
         .def("is_initialized", &sph::SPHEngine::is_initialized)
-        .def("get_positions", [](const sph::SPHEngine& e) { return vec3_array(e.get_positions()); })
-        .def("get_velocities", [](const sph::SPHEngine& e) { return vec3_array(e.get_velocities()); })
-        .def("get_densities", [](const sph::SPHEngine& e) { return float_array(e.get_densities()); })
-        .def("get_pressures", [](const sph::SPHEngine& e) { return float_array(e.get_pressures()); });
+        // the engine's getters, filled in place (the same values as the C++ getters)
+        .def("get_positions", [](const sph::SPHEngine& e) {
+            py::array_t<float> a({e.particle_count(), size_t(3)});
+            e.copy_positions(a.mutable_data());
+            return a;
+        })
+        .def("get_velocities", [](const sph::SPHEngine& e) {
+            py::array_t<float> a({e.particle_count(), size_t(3)});
+            e.copy_velocities(a.mutable_data());
+            return a;
+        })
+        .def("get_densities", [](const sph::SPHEngine& e) {
+            py::array_t<float> a(e.density_count());
+            e.copy_densities(a.mutable_data());
+            return a;
+        })
+        .def("get_pressures", [](const sph::SPHEngine& e) {
+            py::array_t<float> a(e.density_count());
+            e.copy_pressures(a.mutable_data());
+            return a;
+        });
 
     py::class_<sph::SpatialHash>(m, "SpatialHash")
         .def(py::init<float>(), py::arg("cell_size") = 0.02f)
