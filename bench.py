@@ -29,7 +29,9 @@ describes.  Between timed steps the L2 cache is flushed (a 512 MiB buffer is wri
   extras     e2e_dropin (sph.Simulator step + get_positions + get_densities, host clock),
              batched_256 (the 256-scene mix, batched vs looped plain steps, autotuned, with
              its own trajectory bounded to 30 s and an FP64 density check of 8 scenes in the
-             CPU leg), dam_break_10M (exact and precision mode, fresh-state),
+             CPU leg), dam_break_1M_precise (the same workload in the precision mode:
+             cell + offset storage and the tile sweeps), dam_break_10M (exact and
+             precision mode, fresh-state),
              dam_break_10M_trajectory (the 10M configuration's own 50 CFL steps in precision
              mode with per-step FP64 mass / energy drift, bounded to 60 s of device time),
              dam_break_1M_faithful (the 1M workload's own trajectory with per-step cell
@@ -498,6 +500,40 @@ def bench_dropin(w, steps):
                     "the C++ drop-in SPHEngine, libsph_gb300.so -> libsphx.so)"}
 
 
+def bench_precise(torch, stream, flush, w, steps):
+    """A workload's fresh-state step in the precision mode (cell + FP32 offset storage, the
+    tile sweeps, compensated sums, FP64 CFL and time): device time of the graph-replayed
+    step, with the kernel split from an eager context with phase timers."""
+    import sphx
+
+    out = {}
+    for graph in (True, False):
+        ctx = sphx.Context(w.n, mode=sphx.MODE_PRECISE, graph=graph, profile=not graph)
+        ctx.set_stream(stream.cuda_stream)
+        ctx.set_params(w.params)
+        ctx.upload(w.pos, w.vel, w.mass)
+        ctx.snapshot()
+        for _ in range(3):
+            ctx.restore()
+            ctx.step(w.dt)
+        torch.cuda.synchronize()
+        ctx.reset_stats()
+        ms = timed_steps(torch, ctx, w, steps, flush)
+        if graph:
+            out.update({"value": w.n * steps / (sum(ms) * 1e-3), "unit": UNIT, "steps": steps,
+                        "ms_per_step": sum(ms) / steps})
+        else:
+            st = ctx.stats()
+            out.update({"force_kernel_ms": 1e3 * st["force_computation_time"] / steps,
+                        "density_kernel_ms": 1e3 * st["density_computation_time"] / steps,
+                        "grid_build_ms": 1e3 * st["neighbor_search_time"] / steps})
+        ctx.close()
+    out.update({"mode": "cell + FP32 offset, tile sweeps, compensated sums",
+                "kernels": [PASSES["precise"]["density"], PASSES["precise"]["force"]],
+                "protocol": "fresh-state, the workload's dt, captured graph; L2 flushed"})
+    return out
+
+
 def bench_10m_precise(torch, stream, flush, w10, steps):
     """The 10M dam break in the precision mode (cell + FP32 offset storage, compensated
     sums, FP64 CFL maximum and time, FP64 mass / energy sums every step), fresh-state steps
@@ -693,6 +729,11 @@ def bench_ours(args, world, rank, local):
         ctx.close()
         extra["batched_256"], rho_batched = bench_batched(torch, stream, flush,
                                                           max(3, min(args.steps, 10)))
+    if args.workload == "dam_break_1M" and args.mode == "exact":
+        if not ctx_closed(ctx):
+            ctx.close()
+        extra["dam_break_1M_precise"] = bench_precise(torch, stream, flush, w,
+                                                      max(3, min(args.steps, 10)))
     if args.workload == "dam_break_1M" and not args.no_10m:
         w10 = workload("dam_break_10M")
         ctx.close()

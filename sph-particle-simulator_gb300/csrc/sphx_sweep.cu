@@ -138,7 +138,7 @@ struct SweepDensitySmem {
 };
 
 template <int kKern>
-__global__ void __launch_bounds__(128, 7) k_density_sweep(const StepConst c, const Buffers b,
+__global__ void __launch_bounds__(128, 6) k_density_sweep(const StepConst c, const Buffers b,
                                                           DevState* ds) {
     if (ds->status) return;
     extern __shared__ __align__(16) unsigned char smem_sweep_d[];
@@ -315,7 +315,7 @@ __device__ __forceinline__ void sweep_force_pair(const SweepUnits& U, F2 X, F2 Y
 }
 
 template <bool kIntegrate, int kKern, bool kCut>
-__global__ void __launch_bounds__(128, 6) k_force_sweep(const StepConst c, const Buffers b,
+__global__ void __launch_bounds__(128, 5) k_force_sweep(const StepConst c, const Buffers b,
                                                         DevState* ds) {
     if (ds->status) return;
     extern __shared__ __align__(16) unsigned char smem_sweep_f[];
