@@ -137,7 +137,10 @@ struct SweepDensitySmem {
     float4 zm[16];  // z, z, m, m
 };
 
-template <int kKern>
+// kCut: the search radius is below the support 2h (or the kernel is the Gaussian): W is
+// selected by the neighbour test; otherwise W is already 0 beyond 2h and the test only
+// counts the neighbours.
+template <int kKern, bool kCut>
 __global__ void __launch_bounds__(128, 6) k_density_sweep(const StepConst c, const Buffers b,
                                                           DevState* ds) {
     if (ds->status) return;
@@ -210,7 +213,8 @@ __global__ void __launch_bounds__(128, 6) k_density_sweep(const StepConst c, con
                     const float2 e = upk2(d2.v);
                     const bool ha = e.x <= U.r2, hb = e.y <= U.r2;
                     nn += (uint32_t)ha + (uint32_t)hb;
-                    acc = fma2(F2{u1.y}, keep(ha, hb, sweep_w<kKern>(c, d2)), acc);
+                    const F2 w = sweep_w<kKern>(c, d2);
+                    acc = fma2(F2{u1.y}, kCut ? keep(ha, hb, w) : w, acc);
                 }
                 const float2 a2 = upk2(acc.v);
                 rk.add(a2.x + a2.y);  // compensated across chunks
@@ -453,11 +457,20 @@ void launch_sweep(const LaunchCtx& L, LaunchShapeCache& cache, K kernel, size_t 
     kernel<<<nb, threads, sm, L.stream>>>(c, b, ds);
 }
 
+template <int kKern, bool kCut>
+void launch_density_sweep_v(const LaunchCtx& L, const StepConst& c, const Buffers& b,
+                            DevState* ds) {
+    static LaunchShapeCache cache;
+    launch_sweep(L, cache, k_density_sweep<kKern, kCut>, sizeof(SweepDensitySmem), c, b, ds);
+}
+
 template <int kKern>
 void launch_density_sweep_k(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                             DevState* ds) {
-    static LaunchShapeCache cache;
-    launch_sweep(L, cache, k_density_sweep<kKern>, sizeof(SweepDensitySmem), c, b, ds);
+    if (kKern == SPHX_KERNEL_GAUSSIAN || c.r2 < 4.0f * c.h_sq)
+        launch_density_sweep_v<kKern, true>(L, c, b, ds);
+    else
+        launch_density_sweep_v<kKern, false>(L, c, b, ds);
 }
 
 template <bool kIntegrate, int kKern, bool kCut>
