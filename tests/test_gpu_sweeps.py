@@ -19,7 +19,9 @@ acceleration error per component <= 1e-4 of the sum of the magnitudes of its ter
   the cluster, some with a single neighbour near q = 2, are held to 1e-3 instead: there
   (2 - q)^2 carries the rounding of q relative to 2 - q, in every float evaluation (the
   reference's too), and one term is all of the sum;
-* the tile sizes the autotuner tries.
+* the tile sizes the autotuner tries;
+* a grid folded on every axis (a box far larger than the cell grid): cells that fold
+  together are far apart, so a tile's rows pick up only far (culled) candidates from them.
 """
 import numpy as np
 import pytest
@@ -110,3 +112,27 @@ def test_tile_sizes(port, tile):
     w = I.scaled_dam_break(60_000, seed=24)
     out = precise_fields(w.pos, w.vel, w.mass, w.params, tile=tile)
     check_against_fp64(port, w.pos, w.vel, w.mass, w.params, out)
+
+
+@pytest.mark.parametrize("max_cells", [0, 4096])
+def test_folded_grid(port, max_cells):
+    rng = np.random.default_rng(25)
+    clusters = [np.array(c, np.float32) for c in ((0, 0, 0), (10, 10, 10), (3.3, -7.1, 0.2),
+                                                   (250.0, 0.0, -40.0))]
+    pos = np.concatenate([c + rng.random((3000, 3)).astype(np.float32) * 0.25
+                          for c in clusters])
+    n = pos.shape[0]
+    vel = (0.1 * rng.standard_normal((n, 3))).astype(np.float32)
+    mass = np.full(n, 1e-3, np.float32)
+    prm = I.params16(xmin=-100, xmax=300, ymin=-100, ymax=100, zmin=-100, zmax=100)
+    ctx = sphx.Context(n, mode=sphx.MODE_PRECISE, max_grid_cells=max_cells)
+    ctx.set_params(prm)
+    ctx.upload(pos, vel, mass)
+    ctx.eval()
+    out = ctx.download(pos=False, vel=False)
+    if max_cells:
+        assert ctx.stats()["grid_cells"] <= max(max_cells, 125)
+    ctx.close()
+    counts, _ = port.query(pos, 0.04)
+    check_against_fp64(port, pos, vel, mass, prm, out, sel=counts >= 10)
+    check_against_fp64(port, pos, vel, mass, prm, out, sel=counts < 10, acc_tau=1e-3)
