@@ -239,6 +239,7 @@ void free_all(sphx_ctx* c) {
                     b.key[0], b.key[1], b.val[0], b.val[1],   b.key_s,     b.id_s,
                     b.off,  b.tile_start, b.hist, b.scan_part, b.diag_part, c->ds,
                     c->stage, c->snap_pos, c->snap_vel, c->snap_cell, b.cell4, b.cell4_s,
+                    b.spread_tiles, b.run0,
                     b.scene_of, b.scene_s, b.scenes, b.hitmask, b.tile_slot,
                     c->r_colors, c->r_inst, c->r_keys, c->r_rgba};
     for (void* p : ptrs)
@@ -644,7 +645,9 @@ int sphx_create(sphx_ctx** out, size_t capacity, const sphx_tuning* tuning) {
         (rc = dmalloc(&c->ds, 1)) || (rc = dmalloc(&c->stage, 11 * C)))
         return fail(rc);
     if (c->tuning.mode != SPHX_MODE_EXACT &&
-        ((rc = dmalloc(&b.cell4, C)) || (rc = dmalloc(&b.cell4_s, C))))
+        ((rc = dmalloc(&b.cell4, C)) || (rc = dmalloc(&b.cell4_s, C)) ||
+         (rc = dmalloc(&b.spread_tiles, C)) ||
+         (rc = dmalloc(&b.run0, (size_t)max_cells + 1))))
         return fail(rc);
     // Hit-mask pool (exact mode; the precision mode's sweeps keep no records): 4 records
     // (128 B each) per particle of capacity.  A dense state needs about 1.7-2.6 per particle

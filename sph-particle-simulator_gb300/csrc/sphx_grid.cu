@@ -37,8 +37,8 @@ __global__ void k_begin_step(DevState* ds, int reset_bbox) {
     ds->occupied = 0;
     ds->max_occ = 0;
     ds->n_tiles = 0;
-    ds->work[0] = 0;
-    ds->work[1] = 0;
+    for (int k = 0; k < 4; ++k) ds->work[k] = 0;
+    ds->n_spread = 0;
 }
 
 int launch_begin_step(const LaunchCtx& L, DevState* ds, int reset_bbox) {
@@ -391,13 +391,58 @@ static int launch_cell_zorder(const LaunchCtx& L, const Buffers& b, DevState* ds
     return 1;
 }
 
+// Precision-mode step, single scene: the runs of each cell column.  Cell z of a column
+// starts a run when it is the column's first cell or when the kRunCells cells below it
+// hold fewer than tile_n particles.  A tile whose first particle lies in cell z_a then
+// ends by cell z_a + kRunCells: were it to reach past that cell, cells z_a + 1 ..
+// z_a + kRunCells would lie wholly in it, fewer than tile_n particles, so cell
+// z_a + kRunCells + 1 starts a run.  Dense stretches stay one run.  run0[c] = the first
+// cell of c's run (the last run start at or below c).  One warp per column, a max-scan
+// over its cells 32 at a time.
+__global__ void __launch_bounds__(256) k_column_runs(const uint32_t* __restrict__ off,
+                                                     const DevState* ds, uint32_t tile_n,
+                                                     uint32_t* __restrict__ run0) {
+    if (ds->status) return;
+    const uint32_t d2 = (uint32_t)ds->dim[2];
+    if (d2 == 0) return;
+    const uint32_t ncol = ds->ncells / d2;
+    const int lane = threadIdx.x & 31;
+    const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t col = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); col < ncol;
+         col += nwarps) {
+        const uint32_t cb = col * d2;
+        uint32_t carry = cb;
+        for (uint32_t z0 = 0; z0 < d2; z0 += 32) {
+            const uint32_t z = z0 + (uint32_t)lane;
+            uint32_t v = carry;
+            if (z < d2 && z > (uint32_t)kRunCells &&
+                off[cb + z] - off[cb + z - kRunCells] < tile_n)
+                v = cb + z;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= o) v = max(v, u);
+            }
+            if (z < d2) run0[cb + z] = v;
+            carry = __shfl_sync(0xffffffffu, v, 31);
+        }
+    }
+}
+
+static int launch_column_runs(const LaunchCtx& L, const Buffers& b, DevState* ds, int n) {
+    if (!b.columns || !b.run0 || b.nscenes) return 0;
+    k_column_runs<<<grid_blocks(L, n, 256, 2), 256, 0, L.stream>>>(b.off, ds,
+                                                                   (uint32_t)b.tile_n, b.run0);
+    return 1;
+}
+
 // Shared tail of the grid build: stable sort of the keys, gather into cell-sorted order,
-// cell offsets, (b.columns) z order within the cells, tile list.
+// cell offsets, (b.columns) z order within the cells and column runs, tile list.
 int launch_grid_sort(const LaunchCtx& L, const Buffers& b, DevState* ds, int n, float cs) {
     const int r = launch_radix_sort(L, b, ds, n);
     k_reorder<<<grid_blocks(L, n, 256, 8), 256, 0, L.stream>>>(b, n, ds);
     k_offsets<<<grid_blocks(L, n + 1, 256, 8), 256, 0, L.stream>>>(b.key_s, n, ds, b.off);
-    const int z = launch_cell_zorder(L, b, ds, n, cs);
+    const int z = launch_cell_zorder(L, b, ds, n, cs) + launch_column_runs(L, b, ds, n);
     return 2 + r + z + launch_tile_scan(L, b, ds, n);
 }
 

@@ -68,7 +68,9 @@ struct DevState {
     uint32_t vmax_bits;         // max |v| (float bits) for the CFL rule
     uint32_t occupied;          // occupied cells
     uint32_t max_occ;           // particles in the fullest cell
-    uint32_t work[2];           // tile counters of the density and force passes
+    uint32_t work[4];           // tile counters: density and force passes, and their
+                                // spread-tile kernels (precision mode)
+    uint32_t n_spread;          // precision mode: spread tiles listed this step
     float dt;                   // dt of the current step
     float time;                 // current_time_
     float a0[4];                // accelerations_[0] (persists across steps)
@@ -140,7 +142,17 @@ struct Buffers {
     // the tiles run along cell columns (x, y, *), spanning cells; 0: the reference's
     // insertion order within each cell and tiles within one cell
     int columns = 0;
+    // precision mode: the tiles whose particles lie in cells far apart (listed by the density
+    // sweep, swept by the spread-tile kernels), one entry per tile at most
+    uint32_t* spread_tiles = nullptr;
+    // precision mode, single scene (max_cells + 1): the first cell of each cell's run, the
+    // stretch of its column that one sequence of tiles fills (k_column_runs); null: runs
+    // are whole columns
+    uint32_t* run0 = nullptr;
 };
+// A column run ends before cell z when the kRunCells cells below z hold fewer particles
+// than a tile: no tile of a run then spans more than kRunCells cells past its first one.
+constexpr int kRunCells = 4;
 constexpr uint32_t kNoSlot = 0xffffffffu;
 constexpr uint64_t kNoPairs = ~0ull;  // pair fill: this particle's list is not wanted
 

@@ -236,9 +236,10 @@ int launch_radix_sort(const LaunchCtx& L, const Buffers& b, DevState* ds, int n)
 
 // ---------------------------------------------------------------------------------------
 // tile list: a tile starts at every tile_n-th particle of a cell, or (b.columns) of a cell
-// column (x, y, *), contiguous in cell-sorted order; the non-finite group (key == ncells)
-// is tiled the same way.  A column tile may span several cells: the passes walk the union
-// of its particles' stencils.
+// column (x, y, *) -- of a column run (b.run0, k_column_runs) in a single-scene precision
+// step -- contiguous in cell-sorted order; the non-finite group (key == ncells) is tiled
+// the same way.  A column tile may span several cells: the passes walk the union of its
+// particles' stencils.
 // ---------------------------------------------------------------------------------------
 
 // first cell of the column of cell `key` (the non-finite group is its own column)
@@ -261,13 +262,16 @@ struct TileSrc {
     const DevState* ds;
     const uint32_t* scene_s;  // batched mode (else null)
     const SceneInfo* scenes;
-    uint32_t tile_n;  // particles per tile
-    int columns;      // 1: tiles along cell columns, else within cells
+    uint32_t tile_n;        // particles per tile
+    int columns;            // 1: tiles along cell columns, else within cells
+    const uint32_t* run0;   // columns: the first cell of each cell's run (null: the column)
     __device__ bool active() const { return !ds->status; }
     __device__ uint32_t operator()(uint32_t k) const {
         const uint32_t key = key_s[k];
-        const uint32_t st = off[columns ? column_base(key, k, ds, scene_s, scenes) : key];
-        return (k - st) % tile_n == 0 ? 1u : 0u;
+        uint32_t first = key;
+        if (columns && key < ds->ncells)
+            first = run0 ? run0[key] : column_base(key, k, ds, scene_s, scenes);
+        return (k - off[first]) % tile_n == 0 ? 1u : 0u;
     }
 };
 // Writes the tile starts and counts the occupied cells and the fullest one (the threads
@@ -295,7 +299,8 @@ struct TileSink {
 int launch_tile_scan(const LaunchCtx& L, const Buffers& b, DevState* ds, int n) {
     const bool batched = b.nscenes > 0;
     const TileSrc src{b.key_s, b.off, ds, batched ? b.scene_s : nullptr,
-                      batched ? b.scenes : nullptr, (uint32_t)b.tile_n, b.columns};
+                      batched ? b.scenes : nullptr, (uint32_t)b.tile_n, b.columns,
+                      batched ? nullptr : b.run0};
     return scan(L, src, TileSink{b.key_s, b.off, b.tile_start, ds},
          (uint32_t)n, b.scan_part, &ds->n_tiles);
 }

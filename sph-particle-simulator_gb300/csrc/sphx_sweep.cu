@@ -133,33 +133,124 @@ __host__ __device__ __forceinline__ float sweep_w_scale(const StepConst& c) {
 struct SweepDensitySmem {
     float4 box_lo, box_hi;  // the tile's box (kept here, not in registers, across the sweep)
     int2 seg[kMaxSegments];
-    float4 xy[16];  // candidates 2p, 2p+1 of the chunk: x, x, y, y (tile frame)
-    float4 zm[16];  // z, z, m, m
+    union {
+        struct {
+            float4 xy[16];  // candidates 2p, 2p+1 of the chunk: x, x, y, y (tile frame)
+            float4 zm[16];  // z, z, m, m
+        };
+        struct {            // a spread tile (sweep_density_spread): candidate j of the chunk
+            int4 scell[32];  // its cell
+            float4 soff[32]; // its offset in sweep units, mass
+        };
+    };
 };
+
+// A tile is spread when one of its particles lies more than kSpreadCells cells from the
+// frame (a folded grid puts far cells together; on an unfolded grid the column runs keep
+// every tile within kRunCells cells of its first particle's cell): frame
+// coordinates that large would carry rounding of the size of their magnitude, so such a
+// tile sweeps with each lane's own cell as its frame (the separation of a pair is
+// (cell_j - cell_t) cs + (o_j - o_t), the cell difference exact), unculled, one candidate
+// pair at a time.  Rare and slow; exact to the same few ulps as a compact tile.
+constexpr int kSpreadCells = 4;
+static_assert(kRunCells <= kSpreadCells, "a run's tiles would be spread");
+// cell difference a - b as a float (wrapping: cells are clamped to +-2^30, so only a pair
+// that far apart can wrap, and it stays far)
+__device__ __forceinline__ float cdiff(int a, int b) {
+    return (float)(int)((unsigned)a - (unsigned)b);
+}
+__device__ __forceinline__ bool far_cell(const int4& c, const int4& f) {
+    return fabsf(cdiff(c.x, f.x)) > kSpreadCells || fabsf(cdiff(c.y, f.y)) > kSpreadCells ||
+           fabsf(cdiff(c.z, f.z)) > kSpreadCells;
+}
+// A spread tile's offset o / h (sweep units) and mass.  The products are rounded on their
+// own (__fmul_rn): the lane's particle and its own staged copy then give a separation of
+// exactly 0, where a product contracted into the difference (fma(o, 1/h, -o')) would leave
+// its rounding error, a separation of ~1e-8 h whose gradient term does not vanish.
+__device__ __forceinline__ float4 spread_off(const float4& o, const SweepUnits& U) {
+    return make_float4(__fmul_rn(o.x, U.inv), __fmul_rn(o.y, U.inv), __fmul_rn(o.z, U.inv),
+                       o.w);
+}
+// separations (sweep units) of candidates a, b from the lane's particle (cell ct, offset ot)
+__device__ __forceinline__ void spread_sep(const SweepUnits& U, const int4& ct, const float4& ot,
+                                           const int4& ca, const float4& oa, const int4& cb,
+                                           const float4& ob, F2& dx, F2& dy, F2& dz) {
+    dx = f2(fmaf(cdiff(ct.x, ca.x), U.cs, ot.x - oa.x), fmaf(cdiff(ct.x, cb.x), U.cs, ot.x - ob.x));
+    dy = f2(fmaf(cdiff(ct.y, ca.y), U.cs, ot.y - oa.y), fmaf(cdiff(ct.y, cb.y), U.cs, ot.y - ob.y));
+    dz = f2(fmaf(cdiff(ct.z, ca.z), U.cs, ot.z - oa.z), fmaf(cdiff(ct.z, cb.z), U.cs, ot.z - ob.z));
+}
+
+// The density sweep of a spread tile: every candidate of every chunk against the lane's
+// particle in the lane's own frame (ct, ot: its cell and offset in sweep units).
+template <int kKern>
+__device__ __forceinline__ void sweep_density_spread(const StepConst& c, const Buffers& b,
+                                                  const SweepUnits& U, SweepDensitySmem* S,
+                                                  int nseg, int lane, bool valid, int4 ct,
+                                                  float4 ot, KSum& rk, uint32_t& nn) {
+    for (int sg = 0; sg < nseg; ++sg) {
+        const int2 se = S->seg[sg];
+        for (int s = se.x; s < se.y; s += 32) {
+            const int m = min(32, se.y - s);
+            __syncwarp();
+            if (lane < m) {
+                const float4 o = b.pos4_s[s + lane];
+                S->scell[lane] = b.cell4_s[s + lane];
+                S->soff[lane] = spread_off(o, U);
+            } else {  // empty slot: far, no mass
+                S->scell[lane] = ct;
+                S->soff[lane] = make_float4(kFar, kFar, kFar, 0.0f);
+            }
+            __syncwarp();
+            F2 acc = f2(0.0f);
+            for (int j = 0; j < m; j += 2) {
+                F2 dx, dy, dz;
+                spread_sep(U, ct, ot, S->scell[j], S->soff[j], S->scell[j + 1], S->soff[j + 1],
+                           dx, dy, dz);
+                const F2 d2 = fma2(dx, dx, fma2(dy, dy, dz * dz));
+                const float2 e = upk2(d2.v);
+                const bool ha = valid && e.x <= U.r2, hb = valid && e.y <= U.r2;
+                nn += (uint32_t)ha + (uint32_t)hb;
+                acc = fma2(f2(S->soff[j].w, S->soff[j + 1].w), keep(ha, hb, sweep_w<kKern>(c, d2)),
+                           acc);
+            }
+            const float2 a2 = upk2(acc.v);
+            rk.add(a2.x + a2.y);
+        }
+    }
+}
 
 // kCut: the search radius is below the support 2h (or the kernel is the Gaussian): W is
 // selected by the neighbour test; otherwise W is already 0 beyond 2h and the test only
 // counts the neighbours.
-template <int kKern, bool kCut>
+// kSpread: the launch over the spread tiles the main launch listed (the main launch skips
+// them), each lane in its own frame; a separate launch keeps that code out of the main one.
+template <int kKern, bool kCut, bool kSpread>
 __global__ void __launch_bounds__(128, 6) k_density_sweep(const StepConst c, const Buffers b,
                                                           DevState* ds) {
-    if (ds->status) return;
+    if (ds->status || (kSpread && ds->n_spread == 0)) return;  // (an empty list: no atomics)
     extern __shared__ __align__(16) unsigned char smem_sweep_d[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     SweepDensitySmem* S = reinterpret_cast<SweepDensitySmem*>(smem_sweep_d) + warp;
-    const uint32_t ntiles = ds->n_tiles;
+    const uint32_t ntiles = kSpread ? ds->n_spread : ds->n_tiles;
+    uint32_t* work = &ds->work[kSpread ? 2 : 0];
     const Geom g = grid_geom(ds);
     const SweepUnits U = sweep_units(c);
     uint32_t my_max = 0;
-    for (uint32_t t = next_tile(&ds->work[0], lane); t < ntiles; t = next_tile(&ds->work[0], lane)) {
+    for (uint32_t t = next_tile(work, lane); t < ntiles; t = next_tile(work, lane)) {
         Tile T;
         float4 xi;
         bool valid;
         int4 frame;
-        tile_setup_cells(c, b, g, b.tile_start[t], lane, T, xi, valid, frame);
+        tile_setup_cells(c, b, g, b.tile_start[kSpread ? b.spread_tiles[t] : t], lane, T, xi,
+                         valid, frame);
         const int i = T.k0 + lane;
-        if (valid && T.cells) xi = frame_pos_h(b.cell4_s[i], frame, b.pos4_s[i], U);
-        {
+        const int4 ct = valid ? b.cell4_s[i] : frame;
+        if (!kSpread && T.cells && __any_sync(kFull, valid && far_cell(ct, frame))) {
+            if (lane == 0) b.spread_tiles[atomicAdd(&ds->n_spread, 1u)] = t;
+            continue;  // swept by the spread launch
+        }
+        if (valid && T.cells) xi = frame_pos_h(ct, frame, b.pos4_s[i], U);
+        if (!kSpread) {
             const TileBox B = tile_box(xi, valid);
             if (lane == 0) {
                 S->box_lo = make_float4(B.lo[0], B.lo[1], B.lo[2], 0.0f);
@@ -171,6 +262,12 @@ __global__ void __launch_bounds__(128, 6) k_density_sweep(const StepConst c, con
         uint32_t nn = 0;
         const int nseg = build_segments(b, g, T, lane, S->seg);
         __syncwarp();
+        if constexpr (kSpread) {
+            const float4 o = valid ? b.pos4_s[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            sweep_density_spread<kKern>(c, b, U, S, nseg, lane, valid, ct,
+                                        spread_off(o, U),
+                                        rk, nn);
+        } else
         for (int sg = 0; sg < nseg; ++sg) {
             const int2 se = S->seg[sg];
             for (int s = se.x; s < se.y; s += 32) {
@@ -241,7 +338,13 @@ __global__ void __launch_bounds__(128, 6) k_density_sweep(const StepConst c, con
 struct SweepForceSmem {
     float4 box_lo, box_hi;  // the tile's box (kept here, not in registers, across the sweep)
     int2 seg[kMaxSegments];
-    float4 xy[16];  // candidates 2p, 2p+1: x, x, y, y (tile frame)
+    union {
+        float4 xy[16];  // candidates 2p, 2p+1: x, x, y, y (tile frame)
+        struct {        // a spread tile: candidate j's cell and offset (sweep units)
+            int4 scell[32];
+            float4 soff[32];
+        };
+    };
     float4 zv[16];  // z, z, vx, vx
     float4 vv[16];  // vy, vy, vz, vz
     float4 pa[16];  // P, P, kg m/(2 rho), kg m/(2 rho)
@@ -267,16 +370,13 @@ __host__ __device__ __forceinline__ float sweep_kl(const StepConst& c) {
 // the terms of non-neighbours by selection (needed when the search radius is below the
 // support, for the Gaussian, and when a staged candidate carries a non-finite velocity or
 // factor, which a zero factor would not cancel).
+// The terms of a candidate pair from the separations x_t - x_j (dx, dy, dz, sweep units)
+// and the candidates' velocities (vx, vy, vz) and factors (P, kg m/(2 rho); va).
 template <int K, bool kMask>
-__device__ __forceinline__ void sweep_force_pair(const SweepUnits& U, F2 X, F2 Y, F2 Z, F2 VX,
-                                                 F2 VY, F2 VZ, F2 PT, const SweepForceSmem* S,
-                                                 int p, F2& Fx, F2& Fy, F2& Fz) {
-    const ulonglong2 u0 = *reinterpret_cast<const ulonglong2*>(&S->xy[p]);
-    const ulonglong2 u1 = *reinterpret_cast<const ulonglong2*>(&S->zv[p]);
-    const ulonglong2 u2 = *reinterpret_cast<const ulonglong2*>(&S->vv[p]);
-    const ulonglong2 u3 = *reinterpret_cast<const ulonglong2*>(&S->pa[p]);
-    const F2 va{*reinterpret_cast<const f32x2*>(&S->va[p])};
-    const F2 dx = X - F2{u0.x}, dy = Y - F2{u0.y}, dz = Z - F2{u1.x};
+__device__ __forceinline__ void sweep_force_terms(const SweepUnits& U, F2 dx, F2 dy, F2 dz,
+                                                  F2 VX, F2 VY, F2 VZ, F2 PT, F2 vx, F2 vy,
+                                                  F2 vz, F2 pj, F2 cpf, F2 va, F2& Fx, F2& Fy,
+                                                  F2& Fz) {
     const F2 d2 = fma2(dx, dx, fma2(dy, dy, dz * dz));
     const float2 e = upk2(d2.v);
     F2 G, L;
@@ -302,9 +402,9 @@ __device__ __forceinline__ void sweep_force_pair(const SweepUnits& U, F2 X, F2 Y
             L = fma2(b2, f2(-2.0f), a);     // a - 4 b
         }
     }
-    F2 cp = (PT + F2{u3.x}) * F2{u3.y} * G;
+    F2 cp = (PT + pj) * cpf * G;
     F2 cv = va * L;
-    F2 dvx = F2{u1.y} - VX, dvy = F2{u2.x} - VY, dvz = F2{u2.y} - VZ;
+    F2 dvx = vx - VX, dvy = vy - VY, dvz = vz - VZ;
     if (kMask) {
         const bool ha = e.x <= U.r2, hb = e.y <= U.r2;
         cp = keep(ha, hb, cp);
@@ -318,26 +418,101 @@ __device__ __forceinline__ void sweep_force_pair(const SweepUnits& U, F2 X, F2 Y
     Fz = fma2(cv, dvz, fma2(cp, dz, Fz));
 }
 
-template <bool kIntegrate, int kKern, bool kCut>
+// Staged pair p (candidates 2p, 2p+1, tile frame) against the lane's particle.
+template <int K, bool kMask>
+__device__ __forceinline__ void sweep_force_pair(const SweepUnits& U, F2 X, F2 Y, F2 Z, F2 VX,
+                                                 F2 VY, F2 VZ, F2 PT, const SweepForceSmem* S,
+                                                 int p, F2& Fx, F2& Fy, F2& Fz) {
+    const ulonglong2 u0 = *reinterpret_cast<const ulonglong2*>(&S->xy[p]);
+    const ulonglong2 u1 = *reinterpret_cast<const ulonglong2*>(&S->zv[p]);
+    const ulonglong2 u2 = *reinterpret_cast<const ulonglong2*>(&S->vv[p]);
+    const ulonglong2 u3 = *reinterpret_cast<const ulonglong2*>(&S->pa[p]);
+    const F2 va{*reinterpret_cast<const f32x2*>(&S->va[p])};
+    sweep_force_terms<K, kMask>(U, X - F2{u0.x}, Y - F2{u0.y}, Z - F2{u1.x}, VX, VY, VZ, PT,
+                                F2{u1.y}, F2{u2.x}, F2{u2.y}, F2{u3.x}, F2{u3.y}, va, Fx, Fy, Fz);
+}
+
+// The force sweep of a spread tile: every candidate of every chunk against the lane's
+// particle in the lane's own frame (ct, ot), masked by the neighbour test.
+template <int kKern>
+__device__ __forceinline__ void sweep_force_spread(const Buffers& b, const SweepUnits& U, float kg,
+                                                float kl, SweepForceSmem* S, int nseg, int lane,
+                                                int4 ct, float4 ot, F2 VX, F2 VY, F2 VZ, F2 PT,
+                                                KSum& Sx, KSum& Sy, KSum& Sz) {
+    for (int sg = 0; sg < nseg; ++sg) {
+        const int2 se = S->seg[sg];
+        for (int s = se.x; s < se.y; s += 32) {
+            const int m = min(32, se.y - s);
+            int4 cl = ct;
+            float4 ol = make_float4(kFar, kFar, kFar, 0.0f), vl = make_float4(0.f, 0.f, 0.f, 0.f),
+                   al = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (lane < m) {
+                const float4 o = b.pos4_s[s + lane];
+                cl = b.cell4_s[s + lane];
+                ol = spread_off(o, U);
+                vl = b.vel4_s[s + lane];
+                al = b.aux4_s[s + lane];
+            }
+            __syncwarp();
+            {
+                const int p = lane >> 1, h = lane & 1;
+                S->scell[lane] = cl;
+                S->soff[lane] = ol;
+                reinterpret_cast<float*>(&S->zv[p])[2 + h] = vl.x;
+                reinterpret_cast<float*>(&S->vv[p])[h] = vl.y;
+                reinterpret_cast<float*>(&S->vv[p])[2 + h] = vl.z;
+                reinterpret_cast<float*>(&S->pa[p])[h] = al.y;
+                reinterpret_cast<float*>(&S->pa[p])[2 + h] = kg * al.z;
+                reinterpret_cast<float*>(&S->va[p])[h] = kl * al.w;
+            }
+            __syncwarp();
+            F2 Fx = f2(0.0f), Fy = f2(0.0f), Fz = f2(0.0f);
+            for (int j = 0; j < m; j += 2) {
+                const int p = j >> 1;
+                F2 dx, dy, dz;
+                spread_sep(U, ct, ot, S->scell[j], S->soff[j], S->scell[j + 1], S->soff[j + 1],
+                           dx, dy, dz);
+                const ulonglong2 u1 = *reinterpret_cast<const ulonglong2*>(&S->zv[p]);
+                const ulonglong2 u2 = *reinterpret_cast<const ulonglong2*>(&S->vv[p]);
+                const ulonglong2 u3 = *reinterpret_cast<const ulonglong2*>(&S->pa[p]);
+                const F2 va{*reinterpret_cast<const f32x2*>(&S->va[p])};
+                sweep_force_terms<kKern, true>(U, dx, dy, dz, VX, VY, VZ, PT, F2{u1.y}, F2{u2.x},
+                                               F2{u2.y}, F2{u3.x}, F2{u3.y}, va, Fx, Fy, Fz);
+            }
+            const float2 fx = upk2(Fx.v), fy = upk2(Fy.v), fz = upk2(Fz.v);
+            Sx.add(fx.x + fx.y);
+            Sy.add(fy.x + fy.y);
+            Sz.add(fz.x + fz.y);
+        }
+    }
+}
+
+// kSpread: the launch over the spread tiles the density launch listed (skipped here).
+template <bool kIntegrate, int kKern, bool kCut, bool kSpread>
 __global__ void __launch_bounds__(128, 5) k_force_sweep(const StepConst c, const Buffers b,
                                                         DevState* ds) {
-    if (ds->status) return;
+    if (ds->status || (kSpread && ds->n_spread == 0)) return;
     extern __shared__ __align__(16) unsigned char smem_sweep_f[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     SweepForceSmem* S = reinterpret_cast<SweepForceSmem*>(smem_sweep_f) + warp;
-    const uint32_t ntiles = ds->n_tiles;
+    const uint32_t ntiles = kSpread ? ds->n_spread : ds->n_tiles;
+    uint32_t* work = &ds->work[kSpread ? 3 : 1];
     const Geom g = grid_geom(ds);
     const SweepUnits U = sweep_units(c);
     const float kg = sweep_kg(c), kl = sweep_kl(c);
-    for (uint32_t t = next_tile(&ds->work[1], lane); t < ntiles; t = next_tile(&ds->work[1], lane)) {
+    for (uint32_t t = next_tile(work, lane); t < ntiles; t = next_tile(work, lane)) {
         Tile T;
         float4 xi;
         bool valid;
         int4 frame;
-        tile_setup_cells(c, b, g, b.tile_start[t], lane, T, xi, valid, frame);
+        tile_setup_cells(c, b, g, b.tile_start[kSpread ? b.spread_tiles[t] : t], lane, T, xi,
+                         valid, frame);
         const int i = T.k0 + lane;
-        if (valid && T.cells) xi = frame_pos_h(b.cell4_s[i], frame, b.pos4_s[i], U);
-        {
+        const int4 ct = valid ? b.cell4_s[i] : frame;
+        if (!kSpread && T.cells && __any_sync(kFull, valid && far_cell(ct, frame)))
+            continue;  // listed by the density launch, swept by the spread launch
+        if (valid && T.cells) xi = frame_pos_h(ct, frame, b.pos4_s[i], U);
+        if (!kSpread) {
             const TileBox B = tile_box(xi, valid);
             if (lane == 0) {
                 S->box_lo = make_float4(B.lo[0], B.lo[1], B.lo[2], 0.0f);
@@ -354,6 +529,12 @@ __global__ void __launch_bounds__(128, 5) k_force_sweep(const StepConst c, const
         KSum Sx, Sy, Sz;  // force sums, compensated across chunks
         const int nseg = build_segments(b, g, T, lane, S->seg);
         __syncwarp();
+        if constexpr (kSpread) {
+            const float4 o = valid ? b.pos4_s[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            sweep_force_spread<kKern>(b, U, kg, kl, S, nseg, lane, ct,
+                                      spread_off(o, U),
+                                      VX, VY, VZ, PT, Sx, Sy, Sz);
+        } else
         for (int sg = 0; sg < nseg; ++sg) {
             const int2 se = S->seg[sg];
             for (int s = se.x; s < se.y; s += 32) {
@@ -460,8 +641,11 @@ void launch_sweep(const LaunchCtx& L, LaunchShapeCache& cache, K kernel, size_t 
 template <int kKern, bool kCut>
 void launch_density_sweep_v(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                             DevState* ds) {
-    static LaunchShapeCache cache;
-    launch_sweep(L, cache, k_density_sweep<kKern, kCut>, sizeof(SweepDensitySmem), c, b, ds);
+    static LaunchShapeCache cache, cache_spread;
+    launch_sweep(L, cache, k_density_sweep<kKern, kCut, false>, sizeof(SweepDensitySmem), c, b,
+                 ds);
+    launch_sweep(L, cache_spread, k_density_sweep<kKern, kCut, true>, sizeof(SweepDensitySmem),
+                 c, b, ds);
 }
 
 template <int kKern>
@@ -476,9 +660,11 @@ void launch_density_sweep_k(const LaunchCtx& L, const StepConst& c, const Buffer
 template <bool kIntegrate, int kKern, bool kCut>
 void launch_force_sweep_v(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                           DevState* ds) {
-    static LaunchShapeCache cache;
-    launch_sweep(L, cache, k_force_sweep<kIntegrate, kKern, kCut>, sizeof(SweepForceSmem), c, b,
-                 ds);
+    static LaunchShapeCache cache, cache_spread;
+    launch_sweep(L, cache, k_force_sweep<kIntegrate, kKern, kCut, false>, sizeof(SweepForceSmem),
+                 c, b, ds);
+    launch_sweep(L, cache_spread, k_force_sweep<kIntegrate, kKern, kCut, true>,
+                 sizeof(SweepForceSmem), c, b, ds);
 }
 
 template <int kKern>
@@ -503,7 +689,7 @@ int launch_density_sweep(const LaunchCtx& L, const StepConst& c, const Buffers& 
     if (c.kern == SPHX_KERNEL_WENDLAND_C2) launch_density_sweep_k<SPHX_KERNEL_WENDLAND_C2>(L, c, b, ds);
     else if (c.kern == SPHX_KERNEL_GAUSSIAN) launch_density_sweep_k<SPHX_KERNEL_GAUSSIAN>(L, c, b, ds);
     else launch_density_sweep_k<SPHX_KERNEL_CUBIC_SPLINE>(L, c, b, ds);
-    return 1;
+    return 2;  // the main and the spread-tile launch
 }
 
 int launch_force_sweep(const LaunchCtx& L, const StepConst& c, const Buffers& b, DevState* ds,
@@ -513,7 +699,7 @@ int launch_force_sweep(const LaunchCtx& L, const StepConst& c, const Buffers& b,
     else if (c.kern == SPHX_KERNEL_GAUSSIAN)
         launch_force_sweep_k<SPHX_KERNEL_GAUSSIAN>(L, c, b, ds, integrate);
     else launch_force_sweep_k<SPHX_KERNEL_CUBIC_SPLINE>(L, c, b, ds, integrate);
-    return 1;
+    return 2;  // the main and the spread-tile launch
 }
 
 }  // namespace sphx

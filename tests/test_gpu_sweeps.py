@@ -21,7 +21,10 @@ acceleration error per component <= 1e-4 of the sum of the magnitudes of its ter
   reference's too), and one term is all of the sum;
 * the tile sizes the autotuner tries;
 * a grid folded on every axis (a box far larger than the cell grid): cells that fold
-  together are far apart, so a tile's rows pick up only far (culled) candidates from them.
+  together are far apart, so a column tile can hold particles of clusters far apart (a
+  spread tile, swept with each lane's own cell as its frame), and its rows pick up far
+  candidates from the folded cells.  The isolated particles of this case and of the
+  collapsed one (a single neighbour: the particle itself) must get exactly no force.
 """
 import numpy as np
 import pytest
