@@ -27,8 +27,8 @@ __global__ void k_batch_begin(SceneInfo* scenes, int nscenes, DevState* ds) {
         ds->occupied = 0;
         ds->max_occ = 0;
         ds->n_tiles = 0;
-        for (int k = 0; k < 4; ++k) ds->work[k] = 0;
-        ds->n_spread = 0;
+        ds->work[0] = 0;
+        ds->work[1] = 0;
     }
     if (s >= nscenes) return;
     SceneInfo& sc = scenes[s];

@@ -206,6 +206,10 @@ void step_const_from_params(const sphx_params& p, size_t n, int kernel, int mode
     s.fp16 = mode == SPHX_MODE_PRECISE_FP16;
     s.cs = p.neighbor_search_radius;
     s.cs_d = (double)p.neighbor_search_radius;
+    s.sw_cs = s.cs * s.rcp_h;  // 2 exactly for r_search = 2h
+    s.sw_r2 = s.r2 * s.rcp_hsq;
+    s.sw_r2m = s.sw_r2 * 1.0001f;
+    s.sw_skip2 = 1e-12f * s.rcp_hsq;
 }
 
 }  // namespace sphx
@@ -239,7 +243,7 @@ void free_all(sphx_ctx* c) {
                     b.key[0], b.key[1], b.val[0], b.val[1],   b.key_s,     b.id_s,
                     b.off,  b.tile_start, b.hist, b.scan_part, b.diag_part, c->ds,
                     c->stage, c->snap_pos, c->snap_vel, c->snap_cell, b.cell4, b.cell4_s,
-                    b.spread_tiles, b.run0,
+                    b.spread_tiles, b.runs,
                     b.scene_of, b.scene_s, b.scenes, b.hitmask, b.tile_slot,
                     c->r_colors, c->r_inst, c->r_keys, c->r_rgba};
     for (void* p : ptrs)
@@ -647,7 +651,7 @@ int sphx_create(sphx_ctx** out, size_t capacity, const sphx_tuning* tuning) {
     if (c->tuning.mode != SPHX_MODE_EXACT &&
         ((rc = dmalloc(&b.cell4, C)) || (rc = dmalloc(&b.cell4_s, C)) ||
          (rc = dmalloc(&b.spread_tiles, C)) ||
-         (rc = dmalloc(&b.run0, (size_t)max_cells + 1))))
+         (rc = dmalloc(&b.runs, (size_t)max_cells + 1))))
         return fail(rc);
     // Hit-mask pool (exact mode; the precision mode's sweeps keep no records): 4 records
     // (128 B each) per particle of capacity.  A dense state needs about 1.7-2.6 per particle

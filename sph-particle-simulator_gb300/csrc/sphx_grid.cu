@@ -37,7 +37,8 @@ __global__ void k_begin_step(DevState* ds, int reset_bbox) {
     ds->occupied = 0;
     ds->max_occ = 0;
     ds->n_tiles = 0;
-    for (int k = 0; k < 4; ++k) ds->work[k] = 0;
+    ds->work[0] = ds->work[1] = 0;
+    ds->spread_work[0] = ds->spread_work[1] = 0;
     ds->n_spread = 0;
 }
 
@@ -392,47 +393,65 @@ static int launch_cell_zorder(const LaunchCtx& L, const Buffers& b, DevState* ds
 }
 
 // Precision-mode step, single scene: the runs of each cell column.  Cell z of a column
-// starts a run when it is the column's first cell or when the kRunCells cells below it
-// hold fewer than tile_n particles.  A tile whose first particle lies in cell z_a then
-// ends by cell z_a + kRunCells: were it to reach past that cell, cells z_a + 1 ..
-// z_a + kRunCells would lie wholly in it, fewer than tile_n particles, so cell
-// z_a + kRunCells + 1 starts a run.  Dense stretches stay one run.  run0[c] = the first
-// cell of c's run (the last run start at or below c).  One warp per column, a max-scan
-// over its cells 32 at a time.
+// starts a run when it is the column's first cell, or when z is a multiple of A =
+// kRunAlign and the W = kRunWindow cells below z hold fewer than tile_n particles.  A tile
+// whose first particle lies in cell z_a then ends by cell z_a + W + A - 1: the first
+// multiple of A at or above z_a + W + 1, z_m, is at most z_a + W + A, and were the tile
+// to reach cell z_m, cells z_m - W .. z_m - 1 would lie wholly in it, fewer than tile_n
+// particles, so z_m starts a run.  Dense stretches stay one run; a sparse one is cut every
+// A cells (a window of one cell and A = 1 would cut it at every cell).  runs[c] = the
+// sorted positions where c's run starts and ends (the off of its first cell and of the
+// next run's).  One warp per column: a max-scan over its cells 32 at a time upward for
+// the starts, a min-scan downward for the ends.
+__device__ __forceinline__ bool run_starts_at(const uint32_t* __restrict__ off, uint32_t cb,
+                                              uint32_t z, uint32_t tile_n) {
+    return z == 0 || (z > (uint32_t)kRunWindow && z % kRunAlign == 0 &&
+                      off[cb + z] - off[cb + z - kRunWindow] < tile_n);
+}
 __global__ void __launch_bounds__(256) k_column_runs(const uint32_t* __restrict__ off,
                                                      const DevState* ds, uint32_t tile_n,
-                                                     uint32_t* __restrict__ run0) {
+                                                     uint2* __restrict__ runs) {
     if (ds->status) return;
-    const uint32_t d2 = (uint32_t)ds->dim[2];
-    if (d2 == 0) return;
-    const uint32_t ncol = ds->ncells / d2;
+    const int d2 = ds->dim[2];
+    if (d2 <= 0) return;
+    const uint32_t ncol = ds->ncells / (uint32_t)d2;
     const int lane = threadIdx.x & 31;
     const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
     for (uint32_t col = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); col < ncol;
          col += nwarps) {
-        const uint32_t cb = col * d2;
-        uint32_t carry = cb;
-        for (uint32_t z0 = 0; z0 < d2; z0 += 32) {
-            const uint32_t z = z0 + (uint32_t)lane;
-            uint32_t v = carry;
-            if (z < d2 && z > (uint32_t)kRunCells &&
-                off[cb + z] - off[cb + z - kRunCells] < tile_n)
-                v = cb + z;
+        const uint32_t cb = col * (uint32_t)d2;
+        int carry = 0;  // first cell of the run (column-relative)
+        for (int z0 = 0; z0 < d2; z0 += 32) {
+            const int z = z0 + lane;
+            int v = (z < d2 && run_starts_at(off, cb, (uint32_t)z, tile_n)) ? z : carry;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+                const int u = __shfl_up_sync(0xffffffffu, v, o);
                 if (lane >= o) v = max(v, u);
             }
-            if (z < d2) run0[cb + z] = v;
+            if (z < d2) runs[cb + z].x = off[cb + v];
             carry = __shfl_sync(0xffffffffu, v, 31);
+        }
+        carry = d2;  // first cell of the next run (d2: the column's end)
+        for (int z0 = (d2 - 1) & ~31; z0 >= 0; z0 -= 32) {
+            const int z = z0 + lane;
+            int v = (z + 1 < d2 && run_starts_at(off, cb, (uint32_t)(z + 1), tile_n)) ? z + 1
+                                                                                     : carry;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_down_sync(0xffffffffu, v, o);
+                if (lane + o < 32) v = min(v, u);
+            }
+            if (z < d2) runs[cb + z].y = off[cb + v];
+            carry = __shfl_sync(0xffffffffu, v, 0);
         }
     }
 }
 
 static int launch_column_runs(const LaunchCtx& L, const Buffers& b, DevState* ds, int n) {
-    if (!b.columns || !b.run0 || b.nscenes) return 0;
+    if (!b.columns || !b.runs || b.nscenes) return 0;
     k_column_runs<<<grid_blocks(L, n, 256, 2), 256, 0, L.stream>>>(b.off, ds,
-                                                                   (uint32_t)b.tile_n, b.run0);
+                                                                   (uint32_t)b.tile_n, b.runs);
     return 1;
 }
 

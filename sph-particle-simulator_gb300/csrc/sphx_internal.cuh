@@ -43,6 +43,10 @@ struct StepConst {
     double cs_d;           // the same, as double
     // division by the fixed divisors h and h*h (see xdiv_fixed)
     float rcp_h, rcp_hsq;  // RN(1/h), RN(1/h^2)
+    // the precision sweeps' units (lengths in units of h), read from the kernel parameters
+    // rather than held in registers: cs / h, r^2 / h^2, the same with the box cull's margin,
+    // (1e-6 m / h)^2
+    float sw_cs, sw_r2, sw_r2m, sw_skip2;
     int fast_div_h, fast_div_hsq;  // 1: the one-correction sequence is verified for it
     // smoothing kernel (SPHX_KERNEL_*) and the constants its constructor computes in float
     int kern;
@@ -68,9 +72,7 @@ struct DevState {
     uint32_t vmax_bits;         // max |v| (float bits) for the CFL rule
     uint32_t occupied;          // occupied cells
     uint32_t max_occ;           // particles in the fullest cell
-    uint32_t work[4];           // tile counters: density and force passes, and their
-                                // spread-tile kernels (precision mode)
-    uint32_t n_spread;          // precision mode: spread tiles listed this step
+    uint32_t work[2];           // tile counters of the density and force passes
     float dt;                   // dt of the current step
     float time;                 // current_time_
     float a0[4];                // accelerations_[0] (persists across steps)
@@ -78,6 +80,8 @@ struct DevState {
     double sums[kDiagSums];     // FP64 diagnostics of the state after the last step
     double dt64, time64;        // precision mode: dt and current time in FP64
     unsigned long long vmax64;  // precision mode: max |v| (FP64 bits)
+    uint32_t n_spread;          // precision mode: spread tiles listed this step
+    uint32_t spread_work[2];    // precision mode: tile counters of the spread-tile kernels
 };
 
 // Batched mode: one record per scene (device memory).  Scenes are contiguous ranges of
@@ -145,14 +149,16 @@ struct Buffers {
     // precision mode: the tiles whose particles lie in cells far apart (listed by the density
     // sweep, swept by the spread-tile kernels), one entry per tile at most
     uint32_t* spread_tiles = nullptr;
-    // precision mode, single scene (max_cells + 1): the first cell of each cell's run, the
-    // stretch of its column that one sequence of tiles fills (k_column_runs); null: runs
-    // are whole columns
-    uint32_t* run0 = nullptr;
+    // precision mode, single scene (max_cells + 1): per cell, the sorted positions where its
+    // column run -- the stretch of its column that one sequence of tiles fills
+    // (k_column_runs) -- starts and ends; null: runs are whole columns
+    uint2* runs = nullptr;
 };
-// A column run ends before cell z when the kRunCells cells below z hold fewer particles
-// than a tile: no tile of a run then spans more than kRunCells cells past its first one.
-constexpr int kRunCells = 4;
+// A column run ends before cell z when z is a multiple of kRunAlign and the kRunWindow
+// cells below z hold fewer particles than a tile: no tile of a run then reaches more than
+// kRunCells = kRunWindow + kRunAlign - 1 cells past its first one (k_column_runs).
+constexpr int kRunWindow = 2, kRunAlign = 3;
+constexpr int kRunCells = kRunWindow + kRunAlign - 1;
 constexpr uint32_t kNoSlot = 0xffffffffu;
 constexpr uint64_t kNoPairs = ~0ull;  // pair fill: this particle's list is not wanted
 

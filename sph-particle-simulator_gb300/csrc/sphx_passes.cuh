@@ -65,18 +65,13 @@ __device__ __forceinline__ Geom scene_geom(const SceneInfo& sc, const DevState* 
 }
 
 // End (sorted position) of the run a tile of cell `key` may fill: the cell, or (b.columns)
-// its cell column -- its column run where b.run0 marks them (single scene) -- (the
-// non-finite group is its own column).  A run that goes on past cell z + kRunCells holds
-// at least tile_n particles beyond the tile's start, so the search stops there.
+// its cell column -- its column run where b.runs holds them (single scene) -- (the
+// non-finite group is its own column).
 __device__ __forceinline__ uint32_t tile_run_end(const Buffers& b, const Geom& g, uint32_t key) {
     if (!b.columns || key >= g.sentinel) return b.off[key + 1];
+    if (b.runs && !b.nscenes) return b.runs[key].y;
     const uint32_t d2 = (uint32_t)g.dim[2];
-    const uint32_t z = (key - g.base) % d2, cb = key - z;
-    if (!b.run0 || b.nscenes) return b.off[cb + d2];
-    const uint32_t zl = min(z + (uint32_t)kRunCells + 1u, d2);
-    for (uint32_t q = z + 1u; q < zl; ++q)
-        if (b.run0[cb + q] == cb + q) return b.off[cb + q];
-    return b.off[cb + zl];
+    return b.off[g.base + ((key - g.base) / d2 + 1u) * d2];
 }
 
 // The tile's z range relative to its first particle's cell: every lane's cell +-1, or +-2

@@ -236,7 +236,7 @@ int launch_radix_sort(const LaunchCtx& L, const Buffers& b, DevState* ds, int n)
 
 // ---------------------------------------------------------------------------------------
 // tile list: a tile starts at every tile_n-th particle of a cell, or (b.columns) of a cell
-// column (x, y, *) -- of a column run (b.run0, k_column_runs) in a single-scene precision
+// column (x, y, *) -- of a column run (b.runs, k_column_runs) in a single-scene precision
 // step -- contiguous in cell-sorted order; the non-finite group (key == ncells) is tiled
 // the same way.  A column tile may span several cells: the passes walk the union of its
 // particles' stencils.
@@ -264,14 +264,15 @@ struct TileSrc {
     const SceneInfo* scenes;
     uint32_t tile_n;        // particles per tile
     int columns;            // 1: tiles along cell columns, else within cells
-    const uint32_t* run0;   // columns: the first cell of each cell's run (null: the column)
+    const uint2* runs;      // columns: each cell's run (null: the whole column)
     __device__ bool active() const { return !ds->status; }
     __device__ uint32_t operator()(uint32_t k) const {
         const uint32_t key = key_s[k];
-        uint32_t first = key;
-        if (columns && key < ds->ncells)
-            first = run0 ? run0[key] : column_base(key, k, ds, scene_s, scenes);
-        return (k - off[first]) % tile_n == 0 ? 1u : 0u;
+        uint32_t st;
+        if (!columns || key >= ds->ncells) st = off[key];
+        else if (runs) st = runs[key].x;
+        else st = off[column_base(key, k, ds, scene_s, scenes)];
+        return (k - st) % tile_n == 0 ? 1u : 0u;
     }
 };
 // Writes the tile starts and counts the occupied cells and the fullest one (the threads
@@ -300,7 +301,7 @@ int launch_tile_scan(const LaunchCtx& L, const Buffers& b, DevState* ds, int n) 
     const bool batched = b.nscenes > 0;
     const TileSrc src{b.key_s, b.off, ds, batched ? b.scene_s : nullptr,
                       batched ? b.scenes : nullptr, (uint32_t)b.tile_n, b.columns,
-                      batched ? nullptr : b.run0};
+                      batched ? nullptr : b.runs};
     return scan(L, src, TileSink{b.key_s, b.off, b.tile_start, ds},
          (uint32_t)n, b.scan_part, &ds->n_tiles);
 }

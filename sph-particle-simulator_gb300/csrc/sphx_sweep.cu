@@ -85,13 +85,7 @@ struct SweepUnits {
     float skip2; // (1e-6 m / h)^2: the Gaussian's pressure-term skip
 };
 __device__ __forceinline__ SweepUnits sweep_units(const StepConst& c) {
-    SweepUnits u;
-    u.inv = c.rcp_h;
-    u.cs = c.cs * c.rcp_h;  // 2 exactly for r_search = 2h
-    u.r2 = c.r2 * c.rcp_hsq;
-    u.r2m = u.r2 * 1.0001f;
-    u.skip2 = 1e-12f * c.rcp_hsq;
-    return u;
+    return SweepUnits{c.rcp_h, c.sw_cs, c.sw_r2, c.sw_r2m, c.sw_skip2};
 }
 // A particle (cell, offset o, mass in o.w) in the tile's frame, in sweep units: the cell
 // difference times the cell size plus the offset scaled, one rounding each (as frame_pos
@@ -133,16 +127,15 @@ __host__ __device__ __forceinline__ float sweep_w_scale(const StepConst& c) {
 struct SweepDensitySmem {
     float4 box_lo, box_hi;  // the tile's box (kept here, not in registers, across the sweep)
     int2 seg[kMaxSegments];
-    union {
-        struct {
-            float4 xy[16];  // candidates 2p, 2p+1 of the chunk: x, x, y, y (tile frame)
-            float4 zm[16];  // z, z, m, m
-        };
-        struct {            // a spread tile (sweep_density_spread): candidate j of the chunk
-            int4 scell[32];  // its cell
-            float4 soff[32]; // its offset in sweep units, mass
-        };
-    };
+    float4 xy[16];  // candidates 2p, 2p+1 of the chunk: x, x, y, y (tile frame)
+    float4 zm[16];  // z, z, m, m
+};
+// The spread tiles' launch (sweep_density_spread) stages whole candidates; its own layout
+// keeps the main launch's shared memory (and so its L1 share) as small as before.
+struct SweepDensitySpreadSmem {
+    int2 seg[kMaxSegments];
+    int4 scell[32];   // candidate j of the chunk: its cell
+    float4 soff[32];  // its offset in sweep units, mass
 };
 
 // A tile is spread when one of its particles lies more than kSpreadCells cells from the
@@ -184,7 +177,8 @@ __device__ __forceinline__ void spread_sep(const SweepUnits& U, const int4& ct, 
 // particle in the lane's own frame (ct, ot: its cell and offset in sweep units).
 template <int kKern>
 __device__ __forceinline__ void sweep_density_spread(const StepConst& c, const Buffers& b,
-                                                  const SweepUnits& U, SweepDensitySmem* S,
+                                                  const SweepUnits& U,
+                                                  SweepDensitySpreadSmem* S,
                                                   int nseg, int lane, bool valid, int4 ct,
                                                   float4 ot, KSum& rk, uint32_t& nn) {
     for (int sg = 0; sg < nseg; ++sg) {
@@ -219,38 +213,50 @@ __device__ __forceinline__ void sweep_density_spread(const StepConst& c, const B
     }
 }
 
+// The density epilogue of the lane's particle: rho, P and the force sweep's per-candidate
+// factors (rho, P, m / (2 rho), (m / rho) mu).
+__device__ __forceinline__ void density_out(const StepConst& c, const Buffers& b, int i,
+                                            bool cells, float mi, const KSum& rk) {
+    const float rho = cells ? rk.value() * sweep_w_scale(c) : xmul(mi, c.w0);
+    const float P = xmul(c.gas, xsub(rho, c.rest));
+    const float mr = xdiv(mi, rho);
+    b.aux4_s[i] = make_float4(rho, P, 0.5f * mr, mr * c.visc);
+}
+
+// A tile with a particle more than kSpreadCells cells from its frame (listed for the
+// spread launch by the density sweep, skipped by both sweeps).
+__device__ __forceinline__ bool spread_tile(const Buffers& b, const Tile& T, int i, bool valid,
+                                            const int4& frame) {
+    return T.cells && __any_sync(kFull, valid && far_cell(b.cell4_s[i], frame));
+}
+
 // kCut: the search radius is below the support 2h (or the kernel is the Gaussian): W is
 // selected by the neighbour test; otherwise W is already 0 beyond 2h and the test only
 // counts the neighbours.
-// kSpread: the launch over the spread tiles the main launch listed (the main launch skips
-// them), each lane in its own frame; a separate launch keeps that code out of the main one.
-template <int kKern, bool kCut, bool kSpread>
+template <int kKern, bool kCut>
 __global__ void __launch_bounds__(128, 6) k_density_sweep(const StepConst c, const Buffers b,
                                                           DevState* ds) {
-    if (ds->status || (kSpread && ds->n_spread == 0)) return;  // (an empty list: no atomics)
+    if (ds->status) return;
     extern __shared__ __align__(16) unsigned char smem_sweep_d[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     SweepDensitySmem* S = reinterpret_cast<SweepDensitySmem*>(smem_sweep_d) + warp;
-    const uint32_t ntiles = kSpread ? ds->n_spread : ds->n_tiles;
-    uint32_t* work = &ds->work[kSpread ? 2 : 0];
+    const uint32_t ntiles = ds->n_tiles;
     const Geom g = grid_geom(ds);
     const SweepUnits U = sweep_units(c);
     uint32_t my_max = 0;
-    for (uint32_t t = next_tile(work, lane); t < ntiles; t = next_tile(work, lane)) {
+    for (uint32_t t = next_tile(&ds->work[0], lane); t < ntiles; t = next_tile(&ds->work[0], lane)) {
         Tile T;
         float4 xi;
         bool valid;
         int4 frame;
-        tile_setup_cells(c, b, g, b.tile_start[kSpread ? b.spread_tiles[t] : t], lane, T, xi,
-                         valid, frame);
+        tile_setup_cells(c, b, g, b.tile_start[t], lane, T, xi, valid, frame);
         const int i = T.k0 + lane;
-        const int4 ct = valid ? b.cell4_s[i] : frame;
-        if (!kSpread && T.cells && __any_sync(kFull, valid && far_cell(ct, frame))) {
+        if (spread_tile(b, T, i, valid, frame)) {
             if (lane == 0) b.spread_tiles[atomicAdd(&ds->n_spread, 1u)] = t;
             continue;  // swept by the spread launch
         }
-        if (valid && T.cells) xi = frame_pos_h(ct, frame, b.pos4_s[i], U);
-        if (!kSpread) {
+        if (valid && T.cells) xi = frame_pos_h(b.cell4_s[i], frame, b.pos4_s[i], U);
+        {
             const TileBox B = tile_box(xi, valid);
             if (lane == 0) {
                 S->box_lo = make_float4(B.lo[0], B.lo[1], B.lo[2], 0.0f);
@@ -262,12 +268,6 @@ __global__ void __launch_bounds__(128, 6) k_density_sweep(const StepConst c, con
         uint32_t nn = 0;
         const int nseg = build_segments(b, g, T, lane, S->seg);
         __syncwarp();
-        if constexpr (kSpread) {
-            const float4 o = valid ? b.pos4_s[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-            sweep_density_spread<kKern>(c, b, U, S, nseg, lane, valid, ct,
-                                        spread_off(o, U),
-                                        rk, nn);
-        } else
         for (int sg = 0; sg < nseg; ++sg) {
             const int2 se = S->seg[sg];
             for (int s = se.x; s < se.y; s += 32) {
@@ -318,11 +318,47 @@ __global__ void __launch_bounds__(128, 6) k_density_sweep(const StepConst c, con
             }
         }
         if (valid) {
-            const float rho = T.cells ? rk.value() * sweep_w_scale(c) : xmul(xi.w, c.w0);
-            const float P = xmul(c.gas, xsub(rho, c.rest));
-            // the per-candidate factors of the force sweep: (rho, P, m / (2 rho), (m / rho) mu)
-            const float mr = xdiv(xi.w, rho);
-            b.aux4_s[i] = make_float4(rho, P, 0.5f * mr, mr * c.visc);
+            density_out(c, b, i, T.cells, xi.w, rk);
+            my_max = max(my_max, nn);
+        }
+        __syncwarp();
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) my_max = max(my_max, __shfl_xor_sync(kFull, my_max, o));
+    if (lane == 0 && my_max) atomicMax(&ds->max_nn, (unsigned long long)my_max);
+}
+
+// The spread tiles the density launch listed, each lane in its own frame (its own launch,
+// so that this code and its shared memory stay out of the main one).
+template <int kKern>
+__global__ void __launch_bounds__(128, 4) k_density_sweep_spread(const StepConst c,
+                                                                 const Buffers b,
+                                                                 DevState* ds) {
+    if (ds->status || ds->n_spread == 0) return;  // (an empty list: no atomics)
+    extern __shared__ __align__(16) unsigned char smem_sweep_ds[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    SweepDensitySpreadSmem* S = reinterpret_cast<SweepDensitySpreadSmem*>(smem_sweep_ds) + warp;
+    const uint32_t ntiles = ds->n_spread;
+    const Geom g = grid_geom(ds);
+    const SweepUnits U = sweep_units(c);
+    uint32_t my_max = 0;
+    for (uint32_t t = next_tile(&ds->spread_work[0], lane); t < ntiles;
+         t = next_tile(&ds->spread_work[0], lane)) {
+        Tile T;
+        float4 xi;
+        bool valid;
+        int4 frame;
+        tile_setup_cells(c, b, g, b.tile_start[b.spread_tiles[t]], lane, T, xi, valid, frame);
+        const int i = T.k0 + lane;
+        const int4 ct = valid ? b.cell4_s[i] : frame;
+        const float4 o = valid ? b.pos4_s[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        KSum rk;
+        uint32_t nn = 0;
+        const int nseg = build_segments(b, g, T, lane, S->seg);
+        __syncwarp();
+        sweep_density_spread<kKern>(c, b, U, S, nseg, lane, valid, ct, spread_off(o, U), rk, nn);
+        if (valid) {
+            density_out(c, b, i, T.cells, xi.w, rk);
             my_max = max(my_max, nn);
         }
         __syncwarp();
@@ -338,17 +374,22 @@ __global__ void __launch_bounds__(128, 6) k_density_sweep(const StepConst c, con
 struct SweepForceSmem {
     float4 box_lo, box_hi;  // the tile's box (kept here, not in registers, across the sweep)
     int2 seg[kMaxSegments];
-    union {
-        float4 xy[16];  // candidates 2p, 2p+1: x, x, y, y (tile frame)
-        struct {        // a spread tile: candidate j's cell and offset (sweep units)
-            int4 scell[32];
-            float4 soff[32];
-        };
-    };
+    float4 xy[16];  // candidates 2p, 2p+1: x, x, y, y (tile frame)
     float4 zv[16];  // z, z, vx, vx
     float4 vv[16];  // vy, vy, vz, vz
     float4 pa[16];  // P, P, kg m/(2 rho), kg m/(2 rho)
     float2 va[16];  // kl (m/rho) mu, kl (m/rho) mu
+};
+// The spread tiles' launch (sweep_force_spread): candidate j's cell and offset (sweep
+// units) in place of the frame coordinates; zv's z slots unused.
+struct SweepForceSpreadSmem {
+    int2 seg[kMaxSegments];
+    int4 scell[32];
+    float4 soff[32];
+    float4 zv[16];
+    float4 vv[16];
+    float4 pa[16];
+    float2 va[16];
 };
 
 // Pressure and viscosity factors of the kernel: the force on particle t from candidate j is
@@ -436,8 +477,9 @@ __device__ __forceinline__ void sweep_force_pair(const SweepUnits& U, F2 X, F2 Y
 // particle in the lane's own frame (ct, ot), masked by the neighbour test.
 template <int kKern>
 __device__ __forceinline__ void sweep_force_spread(const Buffers& b, const SweepUnits& U, float kg,
-                                                float kl, SweepForceSmem* S, int nseg, int lane,
-                                                int4 ct, float4 ot, F2 VX, F2 VY, F2 VZ, F2 PT,
+                                                float kl, SweepForceSpreadSmem* S, int nseg,
+                                                int lane, int4 ct, float4 ot, F2 VX, F2 VY,
+                                                F2 VZ, F2 PT,
                                                 KSum& Sx, KSum& Sy, KSum& Sz) {
     for (int sg = 0; sg < nseg; ++sg) {
         const int2 se = S->seg[sg];
@@ -487,32 +529,56 @@ __device__ __forceinline__ void sweep_force_spread(const Buffers& b, const Sweep
     }
 }
 
-// kSpread: the launch over the spread tiles the density launch listed (skipped here).
-template <bool kIntegrate, int kKern, bool kCut, bool kSpread>
+// The force epilogue of the lane's particle: the acceleration, and (kIntegrate) the
+// leapfrog step with the wall clamp, scattered back to insertion order.
+template <bool kIntegrate>
+__device__ __forceinline__ void force_out(const StepConst& c, const Buffers& b, DevState* ds,
+                                          int i, float mi, const KSum& Sx, const KSum& Sy,
+                                          const KSum& Sz) {
+    const float ax = Sx.value() / mi;
+    const float ay = (Sy.value() + c.grav * mi) / mi;
+    const float az = Sz.value() / mi;
+    b.acc4_s[i] = make_float4(ax, ay, az, 0.0f);
+    if (!kIntegrate) return;
+    const uint32_t id = b.id_s[i];
+    int4 cell = b.cell4_s[i];
+    const float4 own = b.pos4_s[i];
+    const float4 vi = b.vel4_s[i];  // loaded again: not held across the sweep
+    float o[3] = {own.x, own.y, own.z}, v[3] = {vi.x, vi.y, vi.z};
+    const float acc[3] = {ax, ay, az};
+    if (!cell.w) integrate_cells(c, ds->dt, acc, o, v, cell);
+    b.cell4[id] = cell;
+    b.pos4[id] = make_float4(o[0], o[1], o[2], mi);
+    b.vel4[id] = make_float4(v[0], v[1], v[2], 0.0f);
+    if (id == 0) {
+        ds->a0[0] = ax;
+        ds->a0[1] = ay;
+        ds->a0[2] = az;
+    }
+}
+
+template <bool kIntegrate, int kKern, bool kCut>
 __global__ void __launch_bounds__(128, 5) k_force_sweep(const StepConst c, const Buffers b,
                                                         DevState* ds) {
-    if (ds->status || (kSpread && ds->n_spread == 0)) return;
+    if (ds->status) return;
     extern __shared__ __align__(16) unsigned char smem_sweep_f[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     SweepForceSmem* S = reinterpret_cast<SweepForceSmem*>(smem_sweep_f) + warp;
-    const uint32_t ntiles = kSpread ? ds->n_spread : ds->n_tiles;
-    uint32_t* work = &ds->work[kSpread ? 3 : 1];
+    const uint32_t ntiles = ds->n_tiles;
     const Geom g = grid_geom(ds);
     const SweepUnits U = sweep_units(c);
     const float kg = sweep_kg(c), kl = sweep_kl(c);
-    for (uint32_t t = next_tile(work, lane); t < ntiles; t = next_tile(work, lane)) {
+    for (uint32_t t = next_tile(&ds->work[1], lane); t < ntiles; t = next_tile(&ds->work[1], lane)) {
         Tile T;
         float4 xi;
         bool valid;
         int4 frame;
-        tile_setup_cells(c, b, g, b.tile_start[kSpread ? b.spread_tiles[t] : t], lane, T, xi,
-                         valid, frame);
+        tile_setup_cells(c, b, g, b.tile_start[t], lane, T, xi, valid, frame);
         const int i = T.k0 + lane;
-        const int4 ct = valid ? b.cell4_s[i] : frame;
-        if (!kSpread && T.cells && __any_sync(kFull, valid && far_cell(ct, frame)))
+        if (spread_tile(b, T, i, valid, frame))
             continue;  // listed by the density launch, swept by the spread launch
-        if (valid && T.cells) xi = frame_pos_h(ct, frame, b.pos4_s[i], U);
-        if (!kSpread) {
+        if (valid && T.cells) xi = frame_pos_h(b.cell4_s[i], frame, b.pos4_s[i], U);
+        {
             const TileBox B = tile_box(xi, valid);
             if (lane == 0) {
                 S->box_lo = make_float4(B.lo[0], B.lo[1], B.lo[2], 0.0f);
@@ -529,12 +595,6 @@ __global__ void __launch_bounds__(128, 5) k_force_sweep(const StepConst c, const
         KSum Sx, Sy, Sz;  // force sums, compensated across chunks
         const int nseg = build_segments(b, g, T, lane, S->seg);
         __syncwarp();
-        if constexpr (kSpread) {
-            const float4 o = valid ? b.pos4_s[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-            sweep_force_spread<kKern>(b, U, kg, kl, S, nseg, lane, ct,
-                                      spread_off(o, U),
-                                      VX, VY, VZ, PT, Sx, Sy, Sz);
-        } else
         for (int sg = 0; sg < nseg; ++sg) {
             const int2 se = S->seg[sg];
             for (int s = se.x; s < se.y; s += 32) {
@@ -605,27 +665,46 @@ __global__ void __launch_bounds__(128, 5) k_force_sweep(const StepConst c, const
         }
         __syncwarp();
         if (!valid) continue;
-        const float mi = xi.w;
-        const float ax = Sx.value() / mi;
-        const float ay = (Sy.value() + c.grav * mi) / mi;
-        const float az = Sz.value() / mi;
-        b.acc4_s[i] = make_float4(ax, ay, az, 0.0f);
-        if (!kIntegrate) continue;
-        const uint32_t id = b.id_s[i];
-        int4 cell = b.cell4_s[i];
-        const float4 own = b.pos4_s[i];
-        const float4 vi = b.vel4_s[i];  // loaded again: not held across the sweep
-        float o[3] = {own.x, own.y, own.z}, v[3] = {vi.x, vi.y, vi.z};
-        const float acc[3] = {ax, ay, az};
-        if (!cell.w) integrate_cells(c, ds->dt, acc, o, v, cell);
-        b.cell4[id] = cell;
-        b.pos4[id] = make_float4(o[0], o[1], o[2], mi);
-        b.vel4[id] = make_float4(v[0], v[1], v[2], 0.0f);
-        if (id == 0) {
-            ds->a0[0] = ax;
-            ds->a0[1] = ay;
-            ds->a0[2] = az;
+        force_out<kIntegrate>(c, b, ds, i, xi.w, Sx, Sy, Sz);
+    }
+}
+
+// The spread tiles the density launch listed, each lane in its own frame (its own launch).
+template <bool kIntegrate, int kKern>
+__global__ void __launch_bounds__(128, 4) k_force_sweep_spread(const StepConst c,
+                                                               const Buffers b, DevState* ds) {
+    if (ds->status || ds->n_spread == 0) return;
+    extern __shared__ __align__(16) unsigned char smem_sweep_fs[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    SweepForceSpreadSmem* S = reinterpret_cast<SweepForceSpreadSmem*>(smem_sweep_fs) + warp;
+    const uint32_t ntiles = ds->n_spread;
+    const Geom g = grid_geom(ds);
+    const SweepUnits U = sweep_units(c);
+    const float kg = sweep_kg(c), kl = sweep_kl(c);
+    for (uint32_t t = next_tile(&ds->spread_work[1], lane); t < ntiles;
+         t = next_tile(&ds->spread_work[1], lane)) {
+        Tile T;
+        float4 xi;
+        bool valid;
+        int4 frame;
+        tile_setup_cells(c, b, g, b.tile_start[b.spread_tiles[t]], lane, T, xi, valid, frame);
+        const int i = T.k0 + lane;
+        const int4 ct = valid ? b.cell4_s[i] : frame;
+        const float4 o = valid ? b.pos4_s[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        F2 VX, VY, VZ, PT;
+        {
+            const float4 vi = valid ? b.vel4_s[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float Pi = valid ? b.aux4_s[i].y : 0.0f;
+            VX = f2(vi.x), VY = f2(vi.y), VZ = f2(vi.z), PT = f2(Pi);
         }
+        KSum Sx, Sy, Sz;
+        const int nseg = build_segments(b, g, T, lane, S->seg);
+        __syncwarp();
+        sweep_force_spread<kKern>(b, U, kg, kl, S, nseg, lane, ct, spread_off(o, U), VX, VY, VZ,
+                                  PT, Sx, Sy, Sz);
+        __syncwarp();
+        if (!valid) continue;
+        force_out<kIntegrate>(c, b, ds, i, xi.w, Sx, Sy, Sz);
     }
 }
 
@@ -642,9 +721,8 @@ template <int kKern, bool kCut>
 void launch_density_sweep_v(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                             DevState* ds) {
     static LaunchShapeCache cache, cache_spread;
-    launch_sweep(L, cache, k_density_sweep<kKern, kCut, false>, sizeof(SweepDensitySmem), c, b,
-                 ds);
-    launch_sweep(L, cache_spread, k_density_sweep<kKern, kCut, true>, sizeof(SweepDensitySmem),
+    launch_sweep(L, cache, k_density_sweep<kKern, kCut>, sizeof(SweepDensitySmem), c, b, ds);
+    launch_sweep(L, cache_spread, k_density_sweep_spread<kKern>, sizeof(SweepDensitySpreadSmem),
                  c, b, ds);
 }
 
@@ -661,10 +739,10 @@ template <bool kIntegrate, int kKern, bool kCut>
 void launch_force_sweep_v(const LaunchCtx& L, const StepConst& c, const Buffers& b,
                           DevState* ds) {
     static LaunchShapeCache cache, cache_spread;
-    launch_sweep(L, cache, k_force_sweep<kIntegrate, kKern, kCut, false>, sizeof(SweepForceSmem),
-                 c, b, ds);
-    launch_sweep(L, cache_spread, k_force_sweep<kIntegrate, kKern, kCut, true>,
-                 sizeof(SweepForceSmem), c, b, ds);
+    launch_sweep(L, cache, k_force_sweep<kIntegrate, kKern, kCut>, sizeof(SweepForceSmem), c, b,
+                 ds);
+    launch_sweep(L, cache_spread, k_force_sweep_spread<kIntegrate, kKern>,
+                 sizeof(SweepForceSpreadSmem), c, b, ds);
 }
 
 template <int kKern>
