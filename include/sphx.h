@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define SPHX_ABI_VERSION 2
+#define SPHX_ABI_VERSION 3
 
 /* status codes */
 #define SPHX_OK 0
@@ -112,6 +112,10 @@ typedef struct sphx_stats {
     double potential_energy;         /* sum -m g y (gravity acts along y) */
     double sum_density;              /* sum rho_i, FP64 (get_total_mass = sum * h^3) */
     uint64_t kernel_launches;        /* GPU kernels launched by steps/evals of this context */
+    uint32_t tiles;                  /* last step: warp work items (particle tiles) */
+    uint32_t spread_tiles;           /* last step, precision mode: tiles swept in their
+                                        particles' own cell frames (only a folded grid
+                                        yields them) */
 } sphx_stats;
 
 typedef struct sphx_ctx sphx_ctx;

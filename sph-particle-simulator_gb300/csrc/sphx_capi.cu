@@ -1253,6 +1253,8 @@ int sphx_get_stats(sphx_ctx* c, sphx_stats* out) {
     out->potential_energy = s.sums[5];
     out->sum_density = s.sums[6];
     out->kernel_launches = c->launches;
+    out->tiles = s.n_tiles;
+    out->spread_tiles = s.n_spread;
     return s.status;
 }
 

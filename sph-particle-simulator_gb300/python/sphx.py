@@ -85,6 +85,7 @@ class SphxStats(C.Structure):
         ("sum_mass", C.c_double), ("momentum", C.c_double * 3),
         ("kinetic_energy", C.c_double), ("potential_energy", C.c_double),
         ("sum_density", C.c_double), ("kernel_launches", C.c_uint64),
+        ("tiles", C.c_uint32), ("spread_tiles", C.c_uint32),
     ]
 
     def as_dict(self) -> dict:

@@ -32,7 +32,7 @@ def test_library_exports_every_declared_symbol(built):
 
 def test_version_and_error_strings(built):
     lib = sphx.lib()
-    assert lib.sphx_version() == 2
+    assert lib.sphx_version() == 3
     for code in range(-8, 1):
         assert lib.sphx_strerror(code)
 
@@ -42,7 +42,7 @@ def test_struct_layouts_match_header():
     assert C.sizeof(sphx.SphxParams) == 64
     assert [f for f, _ in sphx.SphxParams._fields_][-1] == "neighbor_search_radius"
     assert C.sizeof(sphx.SphxTuning) == 40  # 7 ints + int64
-    assert C.sizeof(sphx.SphxStats) == 5 * 8 + 3 * 8 + 2 * 4 + 4 * 4 + 7 * 8 + 8
+    assert C.sizeof(sphx.SphxStats) == 5 * 8 + 3 * 8 + 2 * 4 + 4 * 4 + 7 * 8 + 8 + 2 * 4
 
 
 def test_null_context_arguments_are_rejected(built):

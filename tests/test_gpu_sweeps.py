@@ -37,12 +37,14 @@ pytestmark = pytest.mark.gpu
 RHO_TOL, ACC_TAU = 1e-5, 1e-4
 
 
-def precise_fields(pos, vel, mass, prm, tile=0):
+def precise_fields(pos, vel, mass, prm, tile=0, stats=None):
     ctx = sphx.Context(max(pos.shape[0], 1), mode=sphx.MODE_PRECISE, tile_particles=tile)
     ctx.set_params(prm)
     ctx.upload(pos, vel, mass)
     ctx.eval()
     out = ctx.download(pos=False, vel=False)
+    if stats is not None:
+        stats.update(ctx.stats())
     ctx.close()
     return out
 
@@ -133,9 +135,34 @@ def test_folded_grid(port, max_cells):
     ctx.upload(pos, vel, mass)
     ctx.eval()
     out = ctx.download(pos=False, vel=False)
+    st = ctx.stats()
     if max_cells:
-        assert ctx.stats()["grid_cells"] <= max(max_cells, 125)
+        assert st["grid_cells"] <= max(max_cells, 125)
+        # a 16^3 fold puts the clusters' cells in shared columns: tiles mix them and take
+        # the spread launches (a CPU count of the same tiles: 64 of 712)
+        assert st["spread_tiles"] > 0
     ctx.close()
     counts, _ = port.query(pos, 0.04)
     check_against_fp64(port, pos, vel, mass, prm, out, sel=counts >= 10)
     check_against_fp64(port, pos, vel, mass, prm, out, sel=counts < 10, acc_tau=1e-3)
+
+
+def test_unfolded_grids_list_no_spread_tiles(built):
+    """On a grid that is not folded the column runs keep every tile within 4 cells of its
+    first particle's cell: no tile takes the spread launches (the dam break's sparse edge
+    columns, a plain lattice, collapsed cells with a sparse rest)."""
+    rng = np.random.default_rng(26)
+    w = I.scaled_dam_break(60_000, seed=26)
+    n = 12_000
+    pos = np.empty((n, 3), np.float32)
+    pos[: n - 2000] = 0.5 + 0.03 * rng.random((n - 2000, 3), dtype=np.float32)
+    pos[n - 2000:] = 0.2 + 0.6 * rng.random((2000, 3), dtype=np.float32)
+    lat = plain_lattice(40)
+    cases = [(w.pos, w.vel, w.mass, w.params),
+             (lat[0], lat[1], lat[2], I.params16()),
+             (pos, np.zeros_like(pos), np.full(n, 1e-3, np.float32), I.params16())]
+    for p, v, m, prm in cases:
+        st = {}
+        precise_fields(p, v, m, prm, stats=st)
+        assert st["tiles"] > 0
+        assert st["spread_tiles"] == 0, st["spread_tiles"]
