@@ -105,7 +105,9 @@ typedef struct sphx_stats {
     uint32_t max_cell_occupancy;     /* last step: particles in the fullest cell */
     uint32_t nonfinite_particles;    /* last step: particles with a NaN/inf coordinate */
     uint32_t grid_cells;             /* last step: cells in the dense grid */
-    /* FP64 reductions over the state after the last step */
+    /* FP64 reductions over the current state (after a step: the state it produced),
+       computed by this call, not by the steps; sum_density over the densities of the
+       last density pass on the current particle set (0 before one) */
     double sum_mass;
     double momentum[3];
     double kinetic_energy;           /* sum 0.5 m |v|^2 */
@@ -216,7 +218,8 @@ typedef struct sphx_scene_stats {
     double kinetic_energy;
     double potential_energy;
 } sphx_scene_stats;
-/* Time, dt and FP64 conservation sums of one scene after the last step (synchronises). */
+/* Time, dt and FP64 conservation sums of one scene after the last step (synchronises; the
+ * sums are computed by this call over the current state, like sphx_get_stats'). */
 int sphx_get_scene_stats(sphx_ctx* ctx, uint32_t scene, sphx_scene_stats* out);
 
 /* Picks the neighbour passes' launch shape for the loaded workload: times two steps of

@@ -24,6 +24,7 @@ struct sphx_ctx {
     sphx_params params{};
     bool have_params = false;
     bool have_fields = false;  // rho/P/acc of the current particle set exist
+    bool diag_stale = false;   // a step ran since the FP64 sums were last computed
     StepConst sc{};
     Buffers b{};
     int kernel = SPHX_KERNEL_CUBIC_SPLINE;
@@ -290,6 +291,28 @@ int sync_status(sphx_ctx* c) {
     return *c->h_status;
 }
 
+// The FP64 sums of the state (k_diag_*, k_batch_diag), computed when the stats are read
+// rather than in every step: the reference's step computes no diagnostics (its
+// get_total_mass / get_total_energy run on demand, src/sph_engine.cpp:187-200).  They
+// cover the current particle state -- after a step, the state it produced -- and the
+// densities of the last density pass (none yet: the density sum is 0).  Not counted in
+// `launches` (the kernels of steps and evals).
+int refresh_diag(sphx_ctx* c) {
+    if (!c->diag_stale) return SPHX_OK;
+    c->diag_stale = false;
+    if (c->n == 0) return SPHX_OK;
+    fill_step_const(c);
+    if (c->b.nscenes > 0) {
+        launch_batch_diag(c->L, c->b, c->ds);
+    } else {
+        Buffers bq = c->b;
+        if (!c->have_fields) bq.aux4_s = nullptr;
+        launch_diag(c->L, c->sc, bq, c->ds);
+    }
+    SPHX_CUDA(cudaGetLastError());
+    return SPHX_OK;
+}
+
 int enter(sphx_ctx* c) {
     if (!c) return SPHX_ERR_INVALID_ARG;
     SPHX_CUDA(cudaSetDevice(c->device));
@@ -323,7 +346,7 @@ int run_phases(sphx_ctx* c, float dt, bool integrate) {
     if (slot) SPHX_CUDA(cudaEventRecord(slot->ev[2], c->stream));
     k += launch_force(c->L, c->sc, c->b, c->ds, integrate ? 1 : 0);
     if (slot) SPHX_CUDA(cudaEventRecord(slot->ev[3], c->stream));
-    if (integrate) k += batch ? launch_batch_diag(c->L, c->b, c->ds) : launch_diag(c->L, c->sc, c->b, c->ds);
+    if (integrate) c->diag_stale = true;  // the FP64 sums: computed when read (refresh_diag)
     if (slot) {
         SPHX_CUDA(cudaEventRecord(slot->ev[4], c->stream));
         slot->pending = true;
@@ -1086,6 +1109,8 @@ int sphx_get_scene_stats(sphx_ctx* c, uint32_t scene, sphx_scene_stats* out) {
     int rc = enter(c);
     if (rc) return rc;
     if (!out || scene >= c->nscenes) return SPHX_ERR_INVALID_ARG;
+    rc = refresh_diag(c);
+    if (rc) return rc;
     SPHX_CUDA(cudaStreamSynchronize(c->stream));
     SceneInfo si;
     SPHX_CUDA(cudaMemcpy(&si, c->b.scenes + scene, sizeof(SceneInfo), cudaMemcpyDeviceToHost));
@@ -1225,6 +1250,8 @@ int sphx_get_stats(sphx_ctx* c, sphx_stats* out) {
     int rc = enter(c);
     if (rc) return rc;
     if (!out) return SPHX_ERR_INVALID_ARG;
+    rc = refresh_diag(c);
+    if (rc) return rc;
     SPHX_CUDA(cudaStreamSynchronize(c->stream));
     rc = drain_all(c);
     if (rc) return rc;

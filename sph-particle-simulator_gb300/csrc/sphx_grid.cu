@@ -487,7 +487,7 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_partial(
         s[4] += 0.5 * m * ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
         const double y = cell4 ? (double)cell4[i].y * cs + (double)p.y : (double)p.y;
         s[5] += -m * (double)grav * y;
-        s[6] += (double)aux4_s[i].x;
+        if (aux4_s) s[6] += (double)aux4_s[i].x;  // null: no density pass on this set yet
     }
     __shared__ double red[kDiagThreads / 32][7];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
