@@ -69,8 +69,8 @@ DENSITY_BYTES_PER_PARTICLE = 24  # read x,m (16 B); write rho,P (8 B)
 # integer cell (12 B) plus an FP32 offset (12 B): force reads x (24), v, rho, P, m (24) and
 # writes x, v, a (48); density reads x, m (28) and writes rho, P (8).
 PASSES = {
-    "exact": {"force": "k_force<1,0,0,0,1,0,0> (force + leapfrog + clamp)",
-              "density": "k_density<0,0,0,1,0>", "force_bytes": FORCE_BYTES_PER_PARTICLE,
+    "exact": {"force": "k_force<1,0,0,1,0,0> (force + leapfrog + clamp)",
+              "density": "k_density<0,0,1,0>", "force_bytes": FORCE_BYTES_PER_PARTICLE,
               "density_bytes": DENSITY_BYTES_PER_PARTICLE, "issue_force": "k_force",
               "issue_density": "k_density", "traffic": "force"},
     "precise": {"force": "k_force_sweep<1,0,0> (force + leapfrog + clamp, tile sweep)",
