@@ -66,3 +66,25 @@ def test_reference_arm_runs_on_rank_zero_only():
 
     args = argparse.Namespace(workload="dam_break_10k", steps=1, warmup=0, gpus=2)
     assert bench.bench_reference(args, world=2, rank=1) == 0  # returns at once, no work
+
+
+def test_reference_arm_line_carries_the_contract_keys(built, capsys):
+    """The reference arm's JSON line on a small workload (rank 0, CPU): its own metric and
+    unit, a cpu_baseline describing the run, and an e2e with no host<->device bytes."""
+    import argparse
+    import json
+
+    import bench
+
+    args = argparse.Namespace(workload="dam_break_10k", steps=1, warmup=0, gpus=1)
+    assert bench.bench_reference(args, world=1, rank=0) == 0
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    assert line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
+    assert line["value"] > 0 and line["higher_is_better"] is True
+    assert line["config"]["workload"] == "dam_break_10k"
+    cb = line["cpu_baseline"]
+    assert cb["value"] == line["value"] and cb["kind"] == "port" and cb["cores"] >= 1
+    assert cb["sample"]
+    assert line["e2e"] == {"value": line["value"], "unit": bench.UNIT,
+                           "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
