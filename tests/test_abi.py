@@ -56,3 +56,34 @@ def test_null_context_arguments_are_rejected(built):
 def test_missing_library_fails_loudly(tmp_path):
     with pytest.raises(ImportError):
         sphx.load_library(tmp_path / "nope.so")
+
+
+def test_ctypes_structs_match_the_c_header(tmp_path):
+    """Every ctypes mirror has the C struct's size and each field's C offset: a small C
+    program compiled against include/sphx.h prints them (a field missing from the header
+    fails the compile)."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    pairs = [(sphx.SphxParams, "sphx_params"), (sphx.SphxTuning, "sphx_tuning"),
+             (sphx.SphxStats, "sphx_stats"), (sphx.SphxSceneStats, "sphx_scene_stats"),
+             (sphx.SphxShape, "sphx_shape"), (sphx.SphxRenderParams, "sphx_render_params")]
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "sphx.h"', "int main(void) {"]
+    expect = []
+    for cls, cname in pairs:
+        lines.append(f'  printf("%zu\\n", sizeof({cname}));')
+        expect.append(C.sizeof(cls))
+        for field, _ in cls._fields_:
+            lines.append(f'  printf("%zu\\n", offsetof({cname}, {field}));')
+            expect.append(getattr(cls, field).offset)
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", f"-I{HEADER.parent}", str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    assert got == expect
