@@ -142,6 +142,18 @@ def test_fp64_checker_agrees_with_the_reference_fields(port, kernel):
     assert err.max() <= 1e-4, err.max()
 
 
+def test_fp64_checker_entry_points_agree(port):
+    """fields_f64d (FP64 positions, the precision study's checker) on positions that are
+    FP32 values gives exactly fields_f64's result: the two entry points are one evaluation."""
+    w = I.config0()
+    rho, P, acc, scale = port.fields_f64(w.pos, w.vel, w.mass, w.params, want_scale=True)
+    rho_d, P_d, acc_d, pairs, scale_d = port.fields_f64d(w.pos.astype(np.float64), w.vel,
+                                                          w.mass, w.params, want_scale=True)
+    for a, b in ((rho, rho_d), (P, P_d), (acc, acc_d), (scale, scale_d)):
+        assert np.array_equal(a, b)
+    assert pairs > w.n  # every particle's own pair and its neighbours
+
+
 def test_port_capacity_drop_and_empty_step(port):
     e = O.Engine(port, 4)
     e.initialize(I.params16())
